@@ -1,0 +1,765 @@
+// GB300 (sm_103a) bidirectional WFA, gap-affine, end-to-end: score + CIGAR on the device.
+//
+// One warp owns one pair at a time; warps pull pair indices from a global work queue
+// (one atomicAdd per pair) so a single persistent launch drains a whole uneven batch.
+// Within a pair, lanes split the diagonals of every wavefront; all control state
+// (scores, breakpoints, recursion) is warp-uniform.
+//
+// Semantics follow WFA2-lib v2.3 exactly (paths relative to WFA2-lib/):
+//   compute      wavefront/wavefront_compute_affine.c:44-86, 229-260; wavefront_compute.c:40-104, 306-632
+//   extend       wavefront/wavefront_extend.c:86-211; wavefront_extend_kernels.c:68-152
+//   termination  wavefront/wavefront_termination.c:37-114
+//   breakpoint   wavefront/wavefront_bialign.c:189-519
+//   recursion    wavefront/wavefront_bialign.c:520-730
+//   leaf         wavefront/wavefront_bialign.c:155-185; wavefront_unialign.c:54-273
+//   backtrace    wavefront/wavefront_backtrace.c:41-219, 320-529
+//   rescoring    alignment/cigar.c:277-303
+#include <climits>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "wfg_internal.h"
+
+namespace wfg {
+namespace {
+
+constexpr int32_t kNull = INT32_MIN / 2;   // WAVEFRONT_OFFSET_NULL
+constexpr int kAbsent = INT32_MAX;         // lo of a wavefront that does not exist
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMaxScope = 32;
+constexpr int ST_OK = -1, ST_END_REACHED = -2, ST_END_UNREACHABLE = -3;
+constexpr int CM = 0, CI = 1, CD = 3;      // components (affine2p_matrix_type values)
+constexpr int kFallbackMinScore = 250, kFallbackMinLength = 100, kRecoveryMinScore = 500;
+constexpr int BT_M = 9, BT_D_EXT = 6, BT_D_OPEN = 5, BT_I_EXT = 2, BT_I_OPEN = 1;
+
+__device__ __forceinline__ int comp_index(int c) { return c == CM ? 0 : (c == CI ? 1 : 2); }
+
+// A view of one stored wavefront. Offsets for diagonal k live at base[(k - kbase) & mask]:
+// rings use kbase = 0 and a power-of-two mask (circular over diagonals), the leaf store
+// uses kbase = the allocation's first diagonal and mask = ~0.
+struct WfRef {
+  int lo, hi;
+  int32_t* base;
+  int kbase;
+  uint32_t mask;
+  __device__ __forceinline__ bool present() const { return lo != kAbsent; }
+  __device__ __forceinline__ bool nonnull() const { return lo <= hi; }
+  __device__ __forceinline__ int32_t at(int k) const { return base[(uint32_t)(k - kbase) & mask]; }
+  __device__ __forceinline__ void put(int k, int32_t v) const { base[(uint32_t)(k - kbase) & mask] = v; }
+  __device__ __forceinline__ int32_t get(int k) const { return (k >= lo && k <= hi) ? at(k) : kNull; }
+};
+
+__device__ __forceinline__ WfRef absent_ref() {
+  WfRef r;
+  r.lo = kAbsent; r.hi = INT_MIN; r.base = nullptr; r.kbase = 0; r.mask = 0;
+  return r;
+}
+
+struct Pen { int x, o, e, scope; };
+
+// Oriented window over packed words (forward arrays for the forward aligner and the
+// leaf, reversed arrays for the reverse aligner).
+struct SeqView {
+  const uint32_t* pw;
+  const uint32_t* tw;
+  int p0, t0;
+  int plen, tlen;
+  int bits;
+};
+
+// 32-bit window of packed characters starting at character pos (first char in the low bits).
+__device__ __forceinline__ uint32_t win32(const uint32_t* w, int pos, int bits) {
+  const uint32_t bit = (uint32_t)pos * (uint32_t)bits;
+  const uint32_t wi = bit >> 5;
+  return __funnelshift_r(w[wi], w[wi + 1], bit & 31u);
+}
+
+// Longest common extension of P[v..] and T[h..] inside the window: the sentinel-bounded
+// blockwise compare of wavefront_extend_matches_kernel_blockwise, with explicit bounds.
+__device__ __forceinline__ int lcp(const SeqView& s, int v, int h) {
+  const int maxn = min(s.plen - v, s.tlen - h);
+  if (maxn <= 0) return 0;
+  const int cpw = 32 / s.bits;
+  int n = 0;
+  for (;;) {
+    const uint32_t x = win32(s.pw, s.p0 + v + n, s.bits) ^ win32(s.tw, s.t0 + h + n, s.bits);
+    if (x) { n += (__ffs((int)x) - 1) / s.bits; break; }
+    n += cpw;
+    if (n >= maxn) break;
+  }
+  return min(n, maxn);
+}
+
+// One direction of WFA over one window (a wavefront_aligner_t in WFA2). Lives in shared
+// memory; every lane updates its fields with identical values.
+struct Dir {
+  int leaf;          // 0: modular ring (breakpoint search), 1: full store (leaf)
+  int scope;
+  int2* rdesc;       // ring descriptors [scope*3] (shared memory)
+  int32_t* rdata;    // ring storage [scope*3][W]
+  int W;
+  int4* ldesc;       // leaf descriptors [(lmax+1)*3] {lo, hi, data_off, kbase}
+  int32_t* ldata;
+  int lcap, lused, lmax;
+  SeqView sv;
+  int cb, ce;
+  int num_null, status, status_score, end_k;
+};
+
+__device__ __forceinline__ WfRef ref_raw(const Dir& d, int score, int ci) {
+  if (score < 0) return absent_ref();
+  WfRef r;
+  if (!d.leaf) {
+    const int slot = score % d.scope;
+    const int2 ds = d.rdesc[slot * 3 + ci];
+    r.lo = ds.x; r.hi = ds.y;
+    r.base = d.rdata + (size_t)(slot * 3 + ci) * (size_t)d.W;
+    r.kbase = 0; r.mask = (uint32_t)d.W - 1u;
+  } else {
+    if (score > d.lmax) return absent_ref();
+    const int4 ds = d.ldesc[score * 3 + ci];
+    r.lo = ds.x; r.hi = ds.y;
+    r.base = d.ldata + ds.z;
+    r.kbase = ds.w; r.mask = 0xffffffffu;
+  }
+  return r;
+}
+// Input fetch: absent when the score is negative, the slot is empty or the wavefront is
+// null (wavefront_compute_get_*wavefront).
+__device__ __forceinline__ WfRef fetch(const Dir& d, int score, int ci) {
+  const WfRef r = ref_raw(d, score, ci);
+  return r.nonnull() ? r : absent_ref();
+}
+__device__ __forceinline__ void set_desc(Dir& d, int score, int ci, int lo, int hi, int data_off, int kbase) {
+  if (!d.leaf) d.rdesc[(score % d.scope) * 3 + ci] = make_int2(lo, hi);
+  else d.ldesc[score * 3 + ci] = make_int4(lo, hi, data_off, kbase);
+}
+
+// wavefront_aligner_init / init_wf (wavefront/wavefront_aligner.c:251-417)
+__device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
+  d.sv = sv; d.cb = cb; d.ce = ce;
+  d.num_null = 0; d.status = ST_OK; d.status_score = 0; d.end_k = INT_MAX;
+  const int cbi = comp_index(cb);
+  if (!d.leaf) {
+    for (int i = 0; i < d.scope * 3; ++i) d.rdesc[i] = make_int2(kAbsent, INT_MIN);
+    d.rdesc[cbi] = make_int2(0, 0);
+    d.rdata[(size_t)cbi * d.W] = 0;  // diagonal 0 of slot 0
+  } else {
+    d.lused = 1;
+    for (int ci = 0; ci < 3; ++ci) d.ldesc[ci] = make_int4(kAbsent, INT_MIN, 0, 0);
+    d.ldesc[cbi] = make_int4(0, 0, 0, 0);
+    d.ldata[0] = 0;
+  }
+}
+
+// wavefront_compute_affine. Returns false when the scratch is too small (the pair is
+// retried with a larger arena).
+__device__ bool dir_compute(Dir& d, const Pen& p, int s, int lane) {
+  if (d.leaf && s > d.lmax) return false;
+  const WfRef mx = fetch(d, s - p.x, 0);
+  const WfRef mo = fetch(d, s - p.o - p.e, 0);
+  const WfRef ie = fetch(d, s - p.e, 1);
+  const WfRef de = fetch(d, s - p.e, 2);
+  const bool hx = mx.nonnull(), ho = mo.nonnull(), hie = ie.nonnull(), hde = de.nonnull();
+  if (!hx && !ho && !hie && !hde) {
+    d.num_null += 1;
+    set_desc(d, s, 0, kAbsent, INT_MIN, 0, 0);
+    set_desc(d, s, 1, kAbsent, INT_MIN, 0, 0);
+    set_desc(d, s, 2, kAbsent, INT_MIN, 0, 0);
+    return true;
+  }
+  d.num_null = 0;
+  // A missing input is the shared null wavefront (lo = 1, hi = -1).
+  int lo = hx ? mx.lo : 1, hi = hx ? mx.hi : -1;
+  lo = min(lo, (ho ? mo.lo : 1) - 1);   hi = max(hi, (ho ? mo.hi : -1) + 1);
+  lo = min(lo, (hie ? ie.lo : 1) + 1);  hi = max(hi, (hie ? ie.hi : -1) + 1);
+  lo = min(lo, (hde ? de.lo : 1) - 1);  hi = max(hi, (hde ? de.hi : -1) - 1);
+  const bool ai = ho || hie, ad = ho || hde;
+  const int width = hi - lo + 1;
+  WfRef om, oi, od;
+  int offm = 0, offi = 0, offd = 0;
+  if (!d.leaf) {
+    if (width > d.W) return false;
+    const int slot = s % d.scope;
+    om.base = d.rdata + (size_t)(slot * 3 + 0) * d.W;
+    oi.base = d.rdata + (size_t)(slot * 3 + 1) * d.W;
+    od.base = d.rdata + (size_t)(slot * 3 + 2) * d.W;
+    om.kbase = oi.kbase = od.kbase = 0;
+    om.mask = oi.mask = od.mask = (uint32_t)d.W - 1u;
+  } else {
+    const int need = width * (1 + (ai ? 1 : 0) + (ad ? 1 : 0));
+    if (d.lused + need > d.lcap) return false;
+    offm = d.lused;
+    offi = offm + width;
+    offd = offi + (ai ? width : 0);
+    d.lused += need;
+    om.base = d.ldata + offm; oi.base = d.ldata + offi; od.base = d.ldata + offd;
+    om.kbase = oi.kbase = od.kbase = lo;
+    om.mask = oi.mask = od.mask = 0xffffffffu;
+  }
+  const uint32_t tl = (uint32_t)d.sv.tlen, pl = (uint32_t)d.sv.plen;
+  int mlo = INT_MAX, mhi = INT_MIN, ilo = INT_MAX, ihi = INT_MIN, dlo = INT_MAX, dhi = INT_MIN;
+  for (int k = lo + lane; k <= hi; k += 32) {
+    const int32_t ins = max(mo.get(k - 1), ie.get(k - 1)) + 1;
+    const int32_t del = max(mo.get(k + 1), de.get(k + 1));
+    const int32_t mis = mx.get(k) + 1;
+    int32_t m = max(del, max(mis, ins));
+    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
+    om.put(k, m);
+    if (m != kNull) { mlo = min(mlo, k); mhi = max(mhi, k); }
+    if (ai) {
+      oi.put(k, ins);
+      if ((uint32_t)ins <= tl && (uint32_t)(ins - k) <= pl) { ilo = min(ilo, k); ihi = max(ihi, k); }
+    }
+    if (ad) {
+      od.put(k, del);
+      if ((uint32_t)del <= tl && (uint32_t)(del - k) <= pl) { dlo = min(dlo, k); dhi = max(dhi, k); }
+    }
+  }
+  // Trim both ends of every output (wavefront_compute_trim_ends): the surviving range is
+  // [min in-bounds k, max in-bounds k]; none in bounds leaves a null wavefront.
+  mlo = __reduce_min_sync(kFull, mlo); mhi = __reduce_max_sync(kFull, mhi);
+  ilo = __reduce_min_sync(kFull, ilo); ihi = __reduce_max_sync(kFull, ihi);
+  dlo = __reduce_min_sync(kFull, dlo); dhi = __reduce_max_sync(kFull, dhi);
+  __syncwarp();
+  if (mlo <= mhi) set_desc(d, s, 0, mlo, mhi, offm, lo); else set_desc(d, s, 0, lo, lo - 1, offm, lo);
+  if (ai) { if (ilo <= ihi) set_desc(d, s, 1, ilo, ihi, offi, lo); else set_desc(d, s, 1, lo, lo - 1, offi, lo); }
+  else set_desc(d, s, 1, kAbsent, INT_MIN, 0, 0);
+  if (ad) { if (dlo <= dhi) set_desc(d, s, 2, dlo, dhi, offd, lo); else set_desc(d, s, 2, lo, lo - 1, offd, lo); }
+  else set_desc(d, s, 2, kAbsent, INT_MIN, 0, 0);
+  return true;
+}
+
+// wavefront_extend_end2end(_max) + wavefront_termination_end2end. Returns 1 when the
+// direction is finished (end reached or unreachable).
+__device__ int dir_extend(Dir& d, int s, int lane, int* max_ak_out) {
+  if (max_ak_out) *max_ak_out = 0;
+  const WfRef m = ref_raw(d, s, 0);
+  if (!m.present()) {
+    if (d.num_null > d.scope) { d.status = ST_END_UNREACHABLE; d.status_score = s; return 1; }
+    return 0;
+  }
+  int my = 0;
+  for (int k = m.lo + lane; k <= m.hi; k += 32) {
+    int32_t off = m.at(k);
+    if (off == kNull) continue;
+    off += lcp(d.sv, off - k, off);
+    m.put(k, off);
+    my = max(my, 2 * off - k);
+  }
+  const int mak = __reduce_max_sync(kFull, my);
+  __syncwarp();
+  const int ak = d.sv.tlen - d.sv.plen;
+  const WfRef t = (d.ce == CM) ? m : ref_raw(d, s, comp_index(d.ce));
+  const bool done = (t.lo <= ak && ak <= t.hi) && (t.at(ak) >= d.sv.tlen);
+  if (done) { d.status = ST_END_REACHED; d.status_score = s; d.end_k = ak; return 1; }
+  if (max_ak_out) *max_ak_out = mak;
+  return 0;
+}
+
+struct BP { int score, sf, sr, kf, kr, of, orv, comp; };
+
+// wavefront_bialign_breakpoint_indel2indel / _m2m: the first k0 (ascending) that meets,
+// found with a ballot per 32 diagonals.
+__device__ void bp_scan(bool is_m, bool fwd, int s0, int s1, const WfRef& w0, const WfRef& w1,
+                        int plen, int tlen, int go, int comp, BP& bp, int lane) {
+  const int lo0 = w0.lo, hi0 = w0.hi;
+  const int lo1 = tlen - plen - w1.hi, hi1 = tlen - plen - w1.lo;
+  if (hi1 < lo0 || hi0 < lo1) return;
+  const int cand = is_m ? s0 + s1 : s0 + s1 - go;
+  if (!(cand < bp.score)) return;
+  const int min_hi = min(hi0, hi1), max_lo = max(lo0, lo1);
+  for (int kb = max_lo; kb <= min_hi; kb += 32) {
+    const int k0 = kb + lane;
+    bool hit = false;
+    int32_t o0 = 0, o1 = 0;
+    if (k0 <= min_hi) {
+      const int k1 = tlen - plen - k0;
+      o0 = w0.at(k0); o1 = w1.at(k1);
+      hit = (o0 + o1 >= tlen);
+      if (hit && !is_m) {
+        const int v = fwd ? o0 - k0 : o1 - k1;
+        const int h = fwd ? o0 : o1;
+        if (v > plen || h > tlen) hit = false;
+      }
+    }
+    const unsigned b = __ballot_sync(kFull, hit);
+    if (b) {
+      const int src = __ffs((int)b) - 1;
+      const int hk0 = __shfl_sync(kFull, k0, src);
+      const int32_t h0 = __shfl_sync(kFull, o0, src);
+      const int32_t h1 = __shfl_sync(kFull, o1, src);
+      const int hk1 = tlen - plen - hk0;
+      if (fwd) { bp.sf = s0; bp.sr = s1; bp.kf = hk0; bp.kr = hk1; bp.of = h0; bp.orv = h1; }
+      else     { bp.sf = s1; bp.sr = s0; bp.kf = hk1; bp.kr = hk0; bp.of = h1; bp.orv = h0; }
+      bp.score = cand;
+      bp.comp = comp;
+      return;
+    }
+  }
+}
+
+// wavefront_bialign_overlap (gap-affine part)
+__device__ void overlap(const Dir& d0, const Dir& d1, int s0, int s1, bool fwd, BP& bp, const Pen& p, int lane) {
+  const int plen = d0.sv.plen, tlen = d0.sv.tlen;
+  const WfRef m0 = ref_raw(d0, s0, 0);
+  if (!m0.present()) return;
+  const WfRef dd0 = ref_raw(d0, s0, 2);
+  const WfRef ii0 = ref_raw(d0, s0, 1);
+  for (int i = 0; i < p.scope; ++i) {
+    const int si = s1 - i;
+    if (si < 0) break;
+    if (s0 + si - p.o >= bp.score) continue;
+    const WfRef dd1 = ref_raw(d1, si, 2);
+    if (dd0.present() && dd1.present()) bp_scan(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, lane);
+    const WfRef ii1 = ref_raw(d1, si, 1);
+    if (ii0.present() && ii1.present()) bp_scan(false, fwd, s0, si, ii0, ii1, plen, tlen, p.o, CI, bp, lane);
+    if (s0 + si >= bp.score) continue;
+    const WfRef mm1 = ref_raw(d1, si, 0);
+    if (mm1.present()) bp_scan(true, fwd, s0, si, m0, mm1, plen, tlen, p.o, CM, bp, lane);
+  }
+}
+
+struct PairSeqs {
+  const uint32_t* pf; const uint32_t* tf; const uint32_t* pr; const uint32_t* tr;
+  int plen, tlen, bits;
+};
+
+__device__ __forceinline__ SeqView fwd_view(const PairSeqs& q, int pb, int pe, int tb, int te) {
+  SeqView v; v.pw = q.pf; v.tw = q.tf; v.p0 = pb; v.t0 = tb; v.plen = pe - pb; v.tlen = te - tb; v.bits = q.bits;
+  return v;
+}
+__device__ __forceinline__ SeqView rev_view(const PairSeqs& q, int pb, int pe, int tb, int te) {
+  SeqView v; v.pw = q.pr; v.tw = q.tr; v.p0 = q.plen - pe; v.t0 = q.tlen - te;
+  v.plen = pe - pb; v.tlen = te - tb; v.bits = q.bits;
+  return v;
+}
+
+// Upper bound on the optimal score of a window (a guard against runaway loops).
+__device__ __forceinline__ int score_guard(const Pen& p, int plen, int tlen) {
+  const int mn = min(plen, tlen), df = abs(plen - tlen);
+  const long long b = (long long)p.x * mn + (long long)(p.o + p.e) + (long long)p.e * df + 4LL * p.scope + 16;
+  return (int)min(b, (long long)INT_MAX / 4);
+}
+
+// wavefront_bialign_find_breakpoint
+__device__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, int pb, int pe, int tb, int te,
+                               int cb, int ce, const Pen& p, int max_steps, BP& bp, int lane, bool& overflow) {
+  dir_init(F, fwd_view(q, pb, pe, tb, te), cb, ce);
+  dir_init(R, rev_view(q, pb, pe, tb, te), ce, cb);
+  __syncwarp();
+  const int plen = pe - pb, tlen = te - tb;
+  const int max_antidiag = plen + tlen - 1;
+  const int guard = score_guard(p, plen, tlen);
+  int sf = 0, sr = 0, fmax = 0, rmax = 0, ak = 0;
+  bp.score = INT_MAX;
+  if (dir_extend(F, sf, lane, &fmax)) return F.status;
+  if (dir_extend(R, sr, lane, &rmax)) return R.status;
+  bool last_fwd = false;
+  for (;;) {
+    if (fmax + rmax >= max_antidiag) break;
+    ++sf;
+    if (!dir_compute(F, p, sf, lane)) { overflow = true; return WFG_ST_SCRATCH_OVERFLOW; }
+    const int qf = dir_extend(F, sf, lane, &ak);
+    if (fmax < ak) fmax = ak;
+    last_fwd = true;
+    if (qf) return F.status;
+    if (fmax + rmax >= max_antidiag) break;
+    ++sr;
+    if (!dir_compute(R, p, sr, lane)) { overflow = true; return WFG_ST_SCRATCH_OVERFLOW; }
+    const int qr = dir_extend(R, sr, lane, &ak);
+    if (rmax < ak) rmax = ak;
+    last_fwd = false;
+    if (qr) return R.status;
+    if (sr + sf >= max_steps) return WFG_ST_MAX_STEPS;
+    if (sf > guard) return WFG_ST_UNATTAINABLE;
+  }
+  for (;;) {
+    if (last_fwd) {
+      const int min_sr = (sr > p.scope - 1) ? sr - (p.scope - 1) : 0;
+      if (sf + min_sr - p.o >= bp.score) break;
+      overlap(F, R, sf, sr, true, bp, p, lane);
+      ++sr;
+      if (!dir_compute(R, p, sr, lane)) { overflow = true; return WFG_ST_SCRATCH_OVERFLOW; }
+      if (dir_extend(R, sr, lane, nullptr)) return R.status;
+    }
+    const int min_sf = (sf > p.scope - 1) ? sf - (p.scope - 1) : 0;
+    if (min_sf + sr - p.o >= bp.score) break;
+    overlap(R, F, sr, sf, false, bp, p, lane);
+    ++sf;
+    if (!dir_compute(F, p, sf, lane)) { overflow = true; return WFG_ST_SCRATCH_OVERFLOW; }
+    if (dir_extend(F, sf, lane, nullptr)) return F.status;
+    if (sr + sf >= max_steps) return WFG_ST_MAX_STEPS;
+    if (sf > guard + 2 * p.scope || sr > guard + 2 * p.scope) return WFG_ST_UNATTAINABLE;
+    last_fwd = true;
+  }
+  return ST_OK;
+}
+
+// Forward run list of the pair (the CIGAR being assembled), with the open run in registers.
+struct RunOut {
+  uint32_t* buf;
+  int n, cap;
+  int cur_op, cur_len;
+  bool overflow;
+  __device__ __forceinline__ void flush() {
+    if (cur_len > 0) {
+      if (n < cap) buf[n] = ((uint32_t)cur_len << 4) | (uint32_t)cur_op; else overflow = true;
+      ++n;
+    }
+    cur_len = 0;
+  }
+  __device__ __forceinline__ void emit(int op, int len) {
+    if (len <= 0) return;
+    if (op == cur_op && cur_len > 0) { cur_len += len; return; }
+    flush();
+    cur_op = op; cur_len = len;
+  }
+};
+
+// wavefront_backtrace_affine: packed (offset<<4)|type source of one step, or the
+// unshifted null when the source is absent or out of range.
+__device__ __forceinline__ long long bt_src(const Dir& B, int score, int ci, int kk, int add, int type) {
+  if (score < 0) return (long long)kNull;
+  const WfRef w = ref_raw(B, score, ci);
+  if (w.lo <= kk && kk <= w.hi) return (long long)(w.at(kk) + add) * 16LL + type;
+  return (long long)kNull;
+}
+
+// Leaf: wavefront_bialign_base -> unialign -> backtrace. Appends the leaf's ops to out.
+__device__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe, int tb, int te, int cb, int ce,
+                          const Pen& p, int max_steps, RunOut& out, uint32_t* lruns, int lruns_cap,
+                          int lane, int* max_leaf_score) {
+  dir_init(B, fwd_view(q, pb, pe, tb, te), cb, ce);
+  __syncwarp();
+  const int guard = score_guard(p, pe - pb, te - tb);
+  int s = 0;
+  for (;;) {
+    if (dir_extend(B, s, lane, nullptr)) break;
+    ++s;
+    if (!dir_compute(B, p, s, lane)) return WFG_ST_SCRATCH_OVERFLOW;
+    if (s >= max_steps) return WFG_ST_UNATTAINABLE;
+    if (s > guard) return WFG_ST_UNATTAINABLE;
+  }
+  if (*max_leaf_score < s) *max_leaf_score = s;
+  if (B.status != ST_END_REACHED) return WFG_ST_UNATTAINABLE;
+  // Backtrace from (end_k, tlen) in component ce; runs are produced end -> begin.
+  const int plen = B.sv.plen, tlen = B.sv.tlen;
+  int nrev = 0; int rop = -1, rlen = 0; bool rover = false;
+  auto push = [&](int op, int len) {
+    if (len <= 0) return;
+    if (op == rop && rlen > 0) { rlen += len; return; }
+    if (rlen > 0) { if (nrev < lruns_cap) lruns[nrev] = ((uint32_t)rlen << 4) | (uint32_t)rop; else rover = true; ++nrev; }
+    rop = op; rlen = len;
+  };
+  int matrix = ce, score = s, k = B.end_k;
+  int32_t off = tlen;
+  int h = off, v = off - k;
+  if (ce == CM) {
+    if (v < plen) push(WFG_OP_DEL, plen - v);
+    if (h < tlen) push(WFG_OP_INS, tlen - h);
+  }
+  int iters = 0;
+  while (v > 0 && h > 0 && score > 0) {
+    if (++iters > plen + tlen + 8) return WFG_ST_UNATTAINABLE;
+    const int mm = score - p.x, go = score - p.o - p.e, ge = score - p.e;
+    long long max_all;
+    if (matrix == CM) {
+      const long long mis = bt_src(B, mm, 0, k, 1, BT_M);
+      const long long io = bt_src(B, go, 0, k - 1, 1, BT_I_OPEN);
+      const long long ix = bt_src(B, ge, 1, k - 1, 1, BT_I_EXT);
+      const long long dop = bt_src(B, go, 0, k + 1, 0, BT_D_OPEN);
+      const long long dx = bt_src(B, ge, 2, k + 1, 0, BT_D_EXT);
+      const long long mi = io >= ix ? io : ix;
+      const long long md = dop >= dx ? dop : dx;
+      const long long mid = mi >= md ? mi : md;
+      max_all = mis >= mid ? mis : mid;
+    } else if (matrix == CI) {
+      const long long io = bt_src(B, go, 0, k - 1, 1, BT_I_OPEN);
+      const long long ix = bt_src(B, ge, 1, k - 1, 1, BT_I_EXT);
+      max_all = io >= ix ? io : ix;
+    } else {
+      const long long dop = bt_src(B, go, 0, k + 1, 0, BT_D_OPEN);
+      const long long dx = bt_src(B, ge, 2, k + 1, 0, BT_D_EXT);
+      max_all = dop >= dx ? dop : dx;
+    }
+    if (max_all < 0) break;
+    if (matrix == CM) {
+      const int max_off = (int)(max_all >> 4);
+      push(WFG_OP_EQ, off - max_off);
+      off = max_off;
+      v = off - k; h = off;
+      if (v <= 0 || h <= 0) break;
+    }
+    const int type = (int)(max_all & 15);
+    if (type == BT_M) { score = mm; matrix = CM; push(WFG_OP_X, 1); --off; }
+    else if (type == BT_I_OPEN) { score = go; matrix = CM; push(WFG_OP_INS, 1); --k; --off; }
+    else if (type == BT_I_EXT) { score = ge; matrix = CI; push(WFG_OP_INS, 1); --k; --off; }
+    else if (type == BT_D_OPEN) { score = go; matrix = CM; push(WFG_OP_DEL, 1); ++k; }
+    else { score = ge; matrix = CD; push(WFG_OP_DEL, 1); ++k; }
+    v = off - k; h = off;
+  }
+  if (matrix == CM) {
+    if (v > 0 && h > 0) {
+      const int nm = min(v, h);
+      push(WFG_OP_EQ, nm);
+      v -= nm; h -= nm;
+    }
+    if (v > 0) push(WFG_OP_DEL, v);
+    if (h > 0) push(WFG_OP_INS, h);
+  } else if (v != 0 || h != 0 || score != 0) {
+    return WFG_ST_UNATTAINABLE;  // WFA2 aborts here ("I?/D?-Beginning backtrace error")
+  }
+  if (rlen > 0) { if (nrev < lruns_cap) lruns[nrev] = ((uint32_t)rlen << 4) | (uint32_t)rop; else rover = true; ++nrev; }
+  if (rover) return WFG_ST_SCRATCH_OVERFLOW;
+  __syncwarp();
+  for (int i = nrev - 1; i >= 0; --i) {
+    const uint32_t r = lruns[i];
+    out.emit((int)(r & 15u), (int)(r >> 4));
+  }
+  return ST_OK;
+}
+
+__device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int match, int x, int o, int e) {
+  int score = 0;
+  for (int i = 0; i < n; ++i) {
+    const int op = (int)(runs[i] & 15u), len = (int)(runs[i] >> 4);
+    if (op == WFG_OP_EQ) score -= match * len;
+    else if (op == WFG_OP_X) score -= x * len;
+    else score -= o + e * len;
+  }
+  return score;
+}
+
+__device__ __forceinline__ int classic_score(int match_o, int plen, int tlen, int wf_score) {
+  const int swg_match = -match_o;
+  if (swg_match == 0) return -wf_score;
+  return (swg_match * (plen + tlen) - wf_score) / 2;
+}
+
+}  // namespace
+
+template <int WPB>
+__global__ void __launch_bounds__(WPB * 32) biwfa_persistent_kernel(KernelParams P) {
+  __shared__ Dir s_dir[WPB][3];
+  __shared__ int2 s_rdesc[WPB][2][kMaxScope * 3];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const long long gwarp = (long long)blockIdx.x * WPB + wib;
+  const ArenaLayout L = wfg_arena_layout(P.scope, P.ring_w, P.leaf_max_score, P.leaf_words,
+                                         P.run_cap, P.leaf_run_cap, P.stack_cap);
+  uint8_t* arena = P.arena + gwarp * P.arena_bytes;
+  int32_t* ring = (int32_t*)(arena + L.ring_off);
+  int4* ldesc = (int4*)(arena + L.ldesc_off);
+  int32_t* ldata = (int32_t*)(arena + L.ldata_off);
+  uint32_t* runs = (uint32_t*)(arena + L.runs_off);
+  uint32_t* lruns = (uint32_t*)(arena + L.lruns_off);
+  int* stack = (int*)(arena + L.stack_off);
+
+  Dir& F = s_dir[wib][0];
+  Dir& R = s_dir[wib][1];
+  Dir& B = s_dir[wib][2];
+  const size_t ring_dir = (size_t)P.scope * 3 * P.ring_w;
+  F.leaf = 0; F.scope = P.scope; F.rdesc = s_rdesc[wib][0]; F.rdata = ring; F.W = P.ring_w;
+  R.leaf = 0; R.scope = P.scope; R.rdesc = s_rdesc[wib][1]; R.rdata = ring + ring_dir; R.W = P.ring_w;
+  B.leaf = 1; B.scope = P.scope; B.ldesc = ldesc; B.ldata = ldata; B.lcap = P.leaf_words; B.lmax = P.leaf_max_score;
+  B.lused = 0;
+  __syncwarp();
+  const Pen pen = {P.x, P.o, P.e, P.scope};
+
+  const unsigned long long num_pairs =
+      P.num_pairs_ptr ? *P.num_pairs_ptr : (unsigned long long)P.num_pairs;
+  for (;;) {
+    unsigned long long widx = 0;
+    if (lane == 0) widx = atomicAdd(P.queue_head, 1ull);
+    widx = __shfl_sync(kFull, widx, 0);
+    if (widx >= num_pairs) break;
+    const int pi = P.order[widx];
+    const PairDesc pd = P.pairs[pi];
+    PairSeqs q;
+    q.pf = P.words + pd.word_off;
+    q.tf = q.pf + pd.pw_len;
+    q.pr = q.tf + pd.tw_len;
+    q.tr = q.pr + pd.pw_len;
+    q.plen = pd.plen; q.tlen = pd.tlen; q.bits = pd.bits;
+    int status = ST_OK;
+    int score = 0;
+    int nsteps = 0, max_leaf = -1, max_depth = 0;
+    RunOut out; out.buf = runs; out.n = 0; out.cap = P.run_cap; out.cur_op = -1; out.cur_len = 0; out.overflow = false;
+
+    if (P.score_only) {
+      // wavefront_bialign_compute_score (wavefront/wavefront_bialign.c:662-699)
+      BP bp; bool ovf = false;
+      const int st = find_breakpoint(F, R, q, 0, q.plen, 0, q.tlen, CM, CM, pen, P.max_steps, bp, lane, ovf);
+      if (st == ST_OK || st == ST_END_REACHED) {
+        const int wf = (st == ST_END_REACHED) ? (F.status == ST_END_REACHED ? F.status_score : R.status_score) : bp.score;
+        score = classic_score(P.match_o, q.plen, q.tlen, wf);
+        status = WFG_ST_COMPLETED;
+      } else {
+        status = st;
+      }
+    } else {
+      // wavefront_bialign (wavefront/wavefront_bialign.c:703-730) with the recursion of
+      // wavefront_bialign_alignment unrolled onto an explicit stack (half_0 before half_1).
+      const bool min_len = max(q.plen, q.tlen) <= kFallbackMinLength;
+      int sp = 0;
+      auto push = [&](int pb, int pe, int tb, int te, int cb, int ce, int rem, int lvl) -> bool {
+        if (sp >= P.stack_cap) return false;
+        int* e = stack + sp * 8;
+        e[0] = pb; e[1] = pe; e[2] = tb; e[3] = te; e[4] = cb; e[5] = ce; e[6] = rem; e[7] = lvl;
+        ++sp;
+        return true;
+      };
+      push(0, q.plen, 0, q.tlen, CM, CM, min_len ? 0 : INT_MAX, 0);
+      while (sp > 0 && status == ST_OK) {
+        --sp;
+        __syncwarp();
+        const int* e = stack + sp * 8;
+        const int pb = e[0], pe = e[1], tb = e[2], te = e[3], cb = e[4], ce = e[5], rem = e[6], lvl = e[7];
+        __syncwarp();
+        if (lvl > max_depth) max_depth = lvl;
+        const int pl = pe - pb, tl = te - tb;
+        if (tl == 0) { out.emit(WFG_OP_DEL, pl); continue; }
+        if (pl == 0) { out.emit(WFG_OP_INS, tl); continue; }
+        if (rem <= kFallbackMinScore) {
+          const int st = leaf_align(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns, P.leaf_run_cap, lane, &max_leaf);
+          if (st != ST_OK) status = st;
+          continue;
+        }
+        BP bp; bool ovf = false;
+        const int st = find_breakpoint(F, R, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, bp, lane, ovf);
+        if (st != ST_OK) {
+          if (st == ST_END_REACHED) {
+            const int reached = (F.status == ST_END_REACHED) ? F.status_score : R.status_score;
+            if (reached <= kRecoveryMinScore) {
+              const int st2 = leaf_align(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns, P.leaf_run_cap, lane, &max_leaf);
+              if (st2 != ST_OK) status = st2;
+            } else {
+              status = WFG_ST_UNATTAINABLE;
+            }
+          } else if (st == WFG_ST_SCRATCH_OVERFLOW || st == WFG_ST_MAX_STEPS || st == WFG_ST_OOM) {
+            status = st;
+          } else {
+            status = WFG_ST_UNATTAINABLE;
+          }
+          continue;
+        }
+        const int bh = bp.of, bv = bp.of - bp.kf;
+        if (!push(pb + bv, pe, tb + bh, te, bp.comp, ce, bp.sr, lvl + 1) ||
+            !push(pb, pb + bv, tb, tb + bh, cb, bp.comp, bp.sf, lvl + 1)) {
+          status = WFG_ST_SCRATCH_OVERFLOW;
+        }
+        __syncwarp();
+      }
+      out.flush();
+      if (status == ST_OK && out.overflow) status = WFG_ST_SCRATCH_OVERFLOW;
+      if (status == ST_OK) status = WFG_ST_COMPLETED;
+      __syncwarp();
+      if (status == WFG_ST_COMPLETED) {
+        score = (out.n > 0) ? rescore_runs(runs, out.n, P.match_o, P.x_o, P.o_o, P.e_o) : 0;
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(P.out_head, (unsigned long long)out.n);
+        base = __shfl_sync(kFull, base, 0);
+        if ((long long)base + out.n > P.out_cap) {
+          status = WFG_ST_OUTPUT_OVERFLOW;
+        } else {
+          for (int i = lane; i < out.n; i += 32) P.out_runs[base + i] = runs[i];
+          if (lane == 0) { P.run_off[pi] = (int64_t)base; P.run_len[pi] = out.n; }
+        }
+      }
+    }
+    if (status == WFG_ST_SCRATCH_OVERFLOW && P.retry_out != nullptr) {
+      // Hand the pair to the next pass (larger arena); its results are written there.
+      if (lane == 0) {
+        const unsigned long long slot = atomicAdd(P.retry_count, 1ull);
+        P.retry_out[slot] = pi;
+      }
+      __syncwarp();
+      continue;
+    }
+    if (lane == 0) {
+      P.scores[pi] = score;
+      P.status[pi] = status;
+      if (status != WFG_ST_COMPLETED) { P.run_off[pi] = 0; P.run_len[pi] = 0; }
+      if (P.stats) {
+        P.stats[pi * 4 + 0] = nsteps;
+        P.stats[pi * 4 + 1] = max_leaf;
+        P.stats[pi * 4 + 2] = max_depth;
+        P.stats[pi * 4 + 3] = 0;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Pack ASCII pairs into the four word arrays per pair; pure ACGT pairs use 2 bits per base,
+// anything else keeps 8 bits so the comparison stays exact for every byte value.
+__global__ void pack_pairs_kernel(int n, const uint8_t* __restrict__ ascii, PairDesc* __restrict__ pairs,
+                                  uint32_t* __restrict__ words) {
+  const int lane = threadIdx.x & 31;
+  const int warps_per_block = blockDim.x >> 5;
+  const long long first = (long long)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const long long stride = (long long)gridDim.x * warps_per_block;
+  for (long long i = first; i < n; i += stride) {
+    PairDesc pd = pairs[i];
+    const uint8_t* P = ascii + pd.p_off;
+    const uint8_t* T = ascii + pd.t_off;
+    bool ok = true;
+    for (int j = lane; j < pd.plen; j += 32) { const uint8_t c = P[j]; ok &= (c == 'A' || c == 'C' || c == 'G' || c == 'T'); }
+    for (int j = lane; j < pd.tlen; j += 32) { const uint8_t c = T[j]; ok &= (c == 'A' || c == 'C' || c == 'G' || c == 'T'); }
+    ok = __all_sync(kFull, ok);
+    const int bits = ok ? 2 : 8;
+    const int cpw = 32 / bits;
+    uint32_t* base = words + pd.word_off;
+    for (int a = 0; a < 4; ++a) {
+      const uint8_t* src = (a & 1) ? T : P;
+      const int len = (a & 1) ? pd.tlen : pd.plen;
+      const bool rev = a >= 2;
+      const int region = (a & 1) ? pd.tw_len : pd.pw_len;
+      uint32_t* dst = base + ((a == 0) ? 0 : (a == 1) ? pd.pw_len : (a == 2) ? pd.pw_len + pd.tw_len : 2 * pd.pw_len + pd.tw_len);
+      for (int w = lane; w < region; w += 32) {
+        uint32_t word = 0;
+        const int c0 = w * cpw;
+        for (int j = 0; j < cpw; ++j) {
+          const int c = c0 + j;
+          if (c >= len) break;
+          const uint8_t ch = rev ? src[len - 1 - c] : src[c];
+          const uint32_t code = (bits == 2) ? (uint32_t)((ch >> 1) & 3u) : (uint32_t)ch;
+          word |= code << (j * bits);
+        }
+        dst[w] = word;
+      }
+    }
+    if (lane == 0) pairs[i].bits = bits;
+  }
+}
+
+// ------------------------------------------------------------------ host launchers
+template <int WPB>
+static cudaError_t launch_biwfa_impl(const KernelParams& p, int grid, cudaStream_t stream) {
+  biwfa_persistent_kernel<WPB><<<grid, WPB * 32, 0, stream>>>(p);
+  return cudaGetLastError();
+}
+
+int biwfa_warps_per_block() { return 4; }
+
+cudaError_t biwfa_occupancy(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<4>, 4 * 32, 0);
+}
+
+cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream) {
+  return launch_biwfa_impl<4>(p, grid, stream);
+}
+
+cudaError_t launch_pack(int n, const uint8_t* ascii, PairDesc* pairs, uint32_t* words, int num_sms,
+                        cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const int wpb = 8;
+  long long blocks = ((long long)n + wpb - 1) / wpb;
+  const long long cap = (long long)num_sms * 16;
+  if (blocks > cap) blocks = cap;
+  pack_pairs_kernel<<<(int)blocks, wpb * 32, 0, stream>>>(n, ascii, pairs, words);
+  return cudaGetLastError();
+}
+
+}  // namespace wfg

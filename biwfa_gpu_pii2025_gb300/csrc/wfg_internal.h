@@ -1,0 +1,112 @@
+// Shared host/device definitions of the GB300 BiWFA engine.
+//
+// Layout in HBM for one batch (all device buffers are owned by a wfg_context_t):
+//   seq_ascii   : the batch's raw pattern/text bytes, concatenated (uploaded once per batch)
+//   seq_words   : per pair, four packed arrays [P fwd | T fwd | P rev | T rev], each
+//                 ceil(len*bits/32)+2 uint32 words (2 zero pad words so a 64-bit window
+//                 read never leaves the array). bits = 2 for pure ACGT pairs, else 8.
+//   arena       : one private scratch slab per resident warp (rings, leaf store, runs, stack)
+//   out_runs    : dense CIGAR output, uint32 (len<<4 | op) SAM-style ops, one contiguous
+//                 span per pair reserved with one atomicAdd when the pair finishes
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define WFG_HD __host__ __device__
+#else
+#define WFG_HD
+#endif
+
+#ifdef __cplusplus
+namespace wfg {
+#endif
+
+// SAM BAM op codes used in the output runs (op '=' is a match, 'X' a mismatch).
+enum { WFG_OP_INS = 1, WFG_OP_DEL = 2, WFG_OP_EQ = 7, WFG_OP_X = 8 };
+
+// Internal per-pair statuses beyond WFA2's public ones.
+enum {
+  WFG_ST_COMPLETED = 0,
+  WFG_ST_MAX_STEPS = -100,
+  WFG_ST_OOM = -200,              // WFA2's WF_STATUS_OOM
+  WFG_ST_UNATTAINABLE = -300,
+  WFG_ST_SCRATCH_OVERFLOW = -210, // the pair needs a larger per-warp arena (retried by the host)
+  WFG_ST_OUTPUT_OVERFLOW = -220,  // the dense output span could not be reserved
+};
+
+struct PairDesc {
+  int64_t word_off;   // first word of this pair's packed arrays in seq_words
+  int64_t p_off;      // pattern / text byte offsets in seq_ascii
+  int64_t t_off;
+  int plen, tlen;
+  int pw_len, tw_len; // words per packed pattern / text array (incl. 2 pad words)
+  int bits;           // 2 or 8 (set by the pack kernel)
+  int pad;
+};
+
+struct KernelParams {
+  // penalties: internal (transformed when match < 0) and the caller's for rescoring
+  int x, o, e, scope;
+  int match_o, x_o, o_o, e_o;
+  int score_only;
+  int max_steps;
+  // pairs
+  int num_pairs;             // used when num_pairs_ptr is null
+  const unsigned long long* num_pairs_ptr; // device count (retry passes read the previous pass's count)
+  const PairDesc* pairs;
+  const int* order;          // processing order (work-stealing queue)
+  int* retry_out;            // pairs that overflowed the arena are appended here (null: final pass)
+  unsigned long long* retry_count;  // append cursor of retry_out
+  unsigned long long* queue_head;   // work-queue cursor of this pass
+  const uint32_t* words;
+  // per-warp arena
+  uint8_t* arena;
+  int64_t arena_bytes;       // bytes per warp
+  int ring_w;                // ring width (power of two, diagonals per wavefront slot)
+  int leaf_words;            // int32 capacity of the leaf wavefront store
+  int leaf_max_score;        // capacity of the leaf descriptor table (scores)
+  int run_cap;               // uint32 capacity of the per-pair run list
+  int leaf_run_cap;          // uint32 capacity of the leaf reverse-run buffer
+  int stack_cap;             // recursion stack entries
+  // outputs
+  int* scores;
+  int* status;
+  int64_t* run_off;
+  int* run_len;
+  uint32_t* out_runs;
+  int64_t out_cap;
+  unsigned long long* out_head;  // dense output cursor (shared by all passes)
+  // statistics (optional, may be null): per pair {n_steps, max_leaf_score, max_depth, n_cells}
+  int* stats;
+};
+
+// Per-warp arena carving (bytes); all offsets 256-byte aligned.
+struct ArenaLayout {
+  int64_t ring_off, ring_bytes;     // 2 directions x scope x 3 components x ring_w int32
+  int64_t ldesc_off, ldesc_bytes;   // (leaf_max_score+1) x 3 x int4
+  int64_t ldata_off, ldata_bytes;   // leaf_words int32
+  int64_t runs_off, runs_bytes;     // run_cap uint32
+  int64_t lruns_off, lruns_bytes;   // leaf_run_cap uint32
+  int64_t stack_off, stack_bytes;   // stack_cap x 8 int32
+  int64_t total;
+};
+
+WFG_HD static inline int64_t wfg_align256(int64_t v) { return (v + 255) & ~(int64_t)255; }
+
+WFG_HD static inline ArenaLayout wfg_arena_layout(int scope, int ring_w, int leaf_max_score, int leaf_words,
+                                           int run_cap, int leaf_run_cap, int stack_cap) {
+  ArenaLayout L;
+  int64_t off = 0;
+  L.ring_off = off; L.ring_bytes = wfg_align256((int64_t)2 * scope * 3 * ring_w * 4); off += L.ring_bytes;
+  L.ldesc_off = off; L.ldesc_bytes = wfg_align256((int64_t)(leaf_max_score + 1) * 3 * 16); off += L.ldesc_bytes;
+  L.ldata_off = off; L.ldata_bytes = wfg_align256((int64_t)leaf_words * 4); off += L.ldata_bytes;
+  L.runs_off = off; L.runs_bytes = wfg_align256((int64_t)run_cap * 4); off += L.runs_bytes;
+  L.lruns_off = off; L.lruns_bytes = wfg_align256((int64_t)leaf_run_cap * 4); off += L.lruns_bytes;
+  L.stack_off = off; L.stack_bytes = wfg_align256((int64_t)stack_cap * 8 * 4); off += L.stack_bytes;
+  L.total = off;
+  return L;
+}
+
+#ifdef __cplusplus
+}  // namespace wfg
+#endif

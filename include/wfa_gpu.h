@@ -1,0 +1,286 @@
+/*
+ * wfa_gpu.h — C ABI of the GB300 BiWFA aligner (libbiwfa_gb300.so).
+ *
+ * Two surfaces:
+ *   1. A source-compatible subset of WFA2-lib v2.3's aligner API, so code written
+ *      against WFA2-lib's BiWFA (gap-affine, wavefront_memory_ultralow) compiles and
+ *      runs unchanged. Each declaration cites the WFA2-lib declaration it replaces
+ *      (paths relative to WFA2-lib/). Scores and CIGARs are bit-identical to WFA2-lib's
+ *      ultralow-memory BiWFA on the same inputs.
+ *   2. A batch API (wfg_*) that carries the GPU throughput path: many pairs per call,
+ *      one persistent work-stealing kernel, CIGARs returned as SAM-style uint32 runs.
+ *
+ * Supported configuration: distance_metric = gap_affine, memory_mode =
+ * wavefront_memory_ultralow, heuristic = wf_heuristic_none, end-to-end form,
+ * match <= 0 (match < 0 via the same penalty transform WFA2-lib applies).
+ * Anything else is refused with WF_STATUS_UNSUPPORTED instead of WFA2-lib's exit(1).
+ * Input bytes must not contain WFA2-lib's sentinel characters '!' (in the text) or
+ * '?' (in the pattern); WFA2-lib's results are undefined there.
+ */
+#ifndef WFA_GPU_H_
+#define WFA_GPU_H_
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+/* wavefront/wfa.h:46-55 */
+#define WF_STATUS_ALG_COMPLETED            0
+#define WF_STATUS_ALG_PARTIAL              1
+#define WF_STATUS_MAX_STEPS_REACHED     -100
+#define WF_STATUS_OOM                   -200
+#define WF_STATUS_UNATTAINABLE          -300
+#define WF_STATUS_OK                      -1
+#define WF_STATUS_END_REACHED             -2
+#define WF_STATUS_END_UNREACHABLE         -3
+/* Added here (no WFA2-lib counterpart): refused configuration, and CUDA errors. */
+#define WF_STATUS_UNSUPPORTED           -400
+#define WF_STATUS_DEVICE_ERROR          -500
+
+/* ------------------------------------------------------------------ attributes */
+/* wavefront/wavefront_penalties.h:42-48 */
+typedef enum {
+  indel = 0, edit = 1, gap_linear = 2, gap_affine = 3, gap_affine_2p = 4
+} distance_metric_t;
+/* wavefront/wavefront_attributes.h:49-52 */
+typedef enum { compute_score, compute_alignment } alignment_scope_t;
+/* wavefront/wavefront_attributes.h:54-58 */
+typedef enum { alignment_end2end, alignment_endsfree } alignment_span_t;
+/* wavefront/wavefront_attributes.h:59-69 */
+typedef struct {
+  alignment_span_t span;
+  bool extension;
+  int pattern_begin_free;
+  int pattern_end_free;
+  int text_begin_free;
+  int text_end_free;
+} alignment_form_t;
+/* alignment/linear_penalties.h */
+typedef struct { int match; int mismatch; int indel; } linear_penalties_t;
+/* alignment/affine_penalties.h:38-43 */
+typedef struct { int match; int mismatch; int gap_opening; int gap_extension; } affine_penalties_t;
+/* alignment/affine2p_penalties.h */
+typedef struct {
+  int match; int mismatch; int gap_opening1; int gap_extension1; int gap_opening2; int gap_extension2;
+} affine2p_penalties_t;
+/* wavefront/wavefront_heuristic.h:41-49 */
+typedef enum {
+  wf_heuristic_none            = 0x0000000000000000ul,
+  wf_heuristic_banded_static   = 0x0000000000000001ul,
+  wf_heuristic_banded_adaptive = 0x0000000000000002ul,
+  wf_heuristic_wfadaptive      = 0x0000000000000004ul,
+  wf_heuristic_xdrop           = 0x0000000000000010ul,
+  wf_heuristic_zdrop           = 0x0000000000000020ul,
+  wf_heuristic_wfmash          = 0x0000000000000040ul,
+} wf_heuristic_strategy;
+/* wavefront/wavefront_heuristic.h:50-69 */
+typedef struct {
+  wf_heuristic_strategy strategy;
+  int steps_between_cutoffs;
+  int min_k; int max_k;
+  int min_wavefront_length; int max_distance_threshold;
+  int xdrop; int zdrop;
+  int steps_wait; int max_sw_score; int max_wf_score; int max_sw_score_offset; int max_sw_score_k;
+} wavefront_heuristic_t;
+/* wavefront/wavefront_attributes.h:104-109 */
+typedef enum {
+  wavefront_memory_high = 0, wavefront_memory_med = 1, wavefront_memory_low = 2, wavefront_memory_ultralow = 3,
+} wavefront_memory_t;
+/* wavefront/wavefront_plot.h (attributes part) */
+typedef struct { bool enabled; int resolution_points; int align_level; } wavefront_plot_attr_t;
+/* wavefront/wavefront_attributes.h:74-99 (the profiler timer is not carried) */
+typedef struct {
+  int max_alignment_steps;
+  int probe_interval_global;
+  int probe_interval_compact;
+  uint64_t max_partial_compacts;
+  uint64_t max_memory_compact;
+  uint64_t max_memory_resident;
+  uint64_t max_memory_abort;
+  int verbose;
+  bool check_alignment_correct;
+  int max_num_threads;
+  int min_offsets_per_thread;
+} alignment_system_t;
+/* wavefront/wavefront_attributes.h:114-133 (mm_allocator is accepted and ignored) */
+typedef struct {
+  distance_metric_t distance_metric;
+  alignment_scope_t alignment_scope;
+  alignment_form_t alignment_form;
+  linear_penalties_t linear_penalties;
+  affine_penalties_t affine_penalties;
+  affine2p_penalties_t affine2p_penalties;
+  wavefront_heuristic_t heuristic;
+  wavefront_memory_t memory_mode;
+  void* mm_allocator;
+  wavefront_plot_attr_t plot;
+  alignment_system_t system;
+} wavefront_aligner_attr_t;
+
+/* wavefront/wavefront_attributes.h:138 (defaults as WFA2-lib's: memory_high + wfadaptive;
+ * callers of the BiWFA path set memory_mode and heuristic explicitly, as with WFA2-lib). */
+extern wavefront_aligner_attr_t wavefront_aligner_attr_default;
+
+/* ------------------------------------------------------------------ results */
+/* alignment/cigar.h:44-58. operations[begin_offset .. end_offset) holds 'M' (match),
+ * 'X' (mismatch), 'I' (insertion), 'D' (deletion). score is the alignment score
+ * (cigar_score_gap_affine of the operations; WFA2-lib leaves INT32_MIN there when
+ * the whole alignment took its unidirectional fallback, this library always fills it). */
+typedef struct {
+  char* operations;
+  int max_operations;
+  int begin_offset;
+  int end_offset;
+  int score;
+  int end_v;
+  int end_h;
+  bool has_misms;
+  uint32_t* cigar_buffer;
+  int cigar_length;
+} cigar_t;
+
+/* wavefront/wfa.h:61-70 (function pointers omitted) */
+typedef struct {
+  int status;
+  int score;
+  bool dropped;
+  int num_null_steps;
+  uint64_t memory_used;
+} wavefront_align_status_t;
+
+/* wavefront/wfa.h:82-112: the public fields WFA2-lib callers read. */
+typedef struct wavefront_aligner_t {
+  wavefront_align_status_t align_status;
+  alignment_scope_t alignment_scope;
+  alignment_form_t alignment_form;
+  wavefront_memory_t memory_mode;
+  cigar_t* cigar;
+  void* impl;             /* private: device context and settings */
+} wavefront_aligner_t;
+
+/* ------------------------------------------------------------------ WFA2-lib subset */
+/* wavefront/wfa.h:125-126; wavefront_aligner.c:421-463. NULL attributes -> defaults.
+ * Returns NULL when no CUDA device is usable. An unsupported configuration still
+ * returns an aligner whose wavefront_align() reports WF_STATUS_UNSUPPORTED. */
+wavefront_aligner_t* wavefront_aligner_new(wavefront_aligner_attr_t* attributes);
+/* wavefront/wfa.h:129-130; wavefront_aligner.c:476-503 */
+void wavefront_aligner_delete(wavefront_aligner_t* const wf_aligner);
+/* wavefront/wfa.h:200-205; wavefront_align.c:578-607. One pair, computed on the GPU.
+ * The result stays in wf_aligner->cigar until the next call. */
+int wavefront_align(wavefront_aligner_t* const wf_aligner,
+                    const char* const pattern, const int pattern_length,
+                    const char* const text, const int text_length);
+/* wavefront/wfa.h:57-58; wavefront_aligner.c:70-97 */
+char* wavefront_align_strerror(const int error_code);
+char* wavefront_align_strerror_short(const int error_code);
+/* wavefront/wfa.h:136-138 (end-to-end is the only supported span) */
+void wavefront_aligner_set_alignment_end_to_end(wavefront_aligner_t* const wf_aligner);
+/* wavefront/wfa.h:148-149 */
+void wavefront_aligner_set_heuristic_none(wavefront_aligner_t* const wf_aligner);
+/* wavefront/wfa.h:176-178 */
+void wavefront_aligner_set_max_alignment_steps(wavefront_aligner_t* const wf_aligner,
+                                               const int max_alignment_steps);
+/* alignment/cigar.h: cigar_sprint (cigar.c:706-740) */
+int cigar_sprint(char* const buffer, const cigar_t* const cigar, const bool print_matches);
+/* alignment/cigar.h: cigar_score_gap_affine (cigar.c:277-303) */
+int cigar_score_gap_affine(const cigar_t* const cigar, const affine_penalties_t* const penalties);
+/* alignment/cigar.h: cigar_get_CIGAR (cigar.c:224-235); SAM BAM op codes, '='/'X' split
+ * when show_mismatches. The buffer belongs to the cigar. */
+void cigar_get_CIGAR(cigar_t* const cigar, const bool show_mismatches,
+                     uint32_t** const cigar_buffer, int* const cigar_length);
+
+/* Batch extension of the WFA2-lib surface (no WFA2-lib counterpart; WFA2-lib callers
+ * loop over wavefront_align, align_benchmark.c:546-551). Aligns num_pairs pairs with
+ * the aligner's settings in one GPU pass. scores/statuses (host arrays of num_pairs)
+ * receive per-pair results; CIGARs are read back with wavefront_batch_cigar. */
+int wavefront_align_batch(wavefront_aligner_t* const wf_aligner, const int num_pairs,
+                          const char* const* patterns, const int* pattern_lengths,
+                          const char* const* texts, const int* text_lengths,
+                          int* scores, int* statuses);
+/* Runs of pair i of the last wavefront_align_batch: *runs points to *num_runs SAM-style
+ * uint32 ops (len<<4 | op, op in {1:I, 2:D, 7:=, 8:X}). Valid until the next call. */
+int wavefront_batch_cigar(wavefront_aligner_t* const wf_aligner, const int pair,
+                          const uint32_t** runs, int* num_runs);
+
+/* ------------------------------------------------------------------ GB300 batch API */
+/* No WFA2-lib counterpart: the throughput path. A context owns one CUDA stream on one
+ * device and grow-only device buffers; it is not thread-safe (one per host thread,
+ * as WFA2-lib aligners). */
+typedef struct wfg_context wfg_context_t;
+
+typedef struct {
+  int match, mismatch, gap_opening, gap_extension; /* caller's penalties (match <= 0) */
+  int score_only;                                  /* 1: score only (compute_score scope) */
+  int max_alignment_steps;                         /* <= 0: unlimited (WFA2 default INT_MAX) */
+} wfg_config_t;
+
+/* Scheduling policy of wfg_run. */
+typedef enum {
+  WFG_SCHED_PLAIN = 0,    /* pairs sorted by length (descending), one arena size for all */
+  WFG_SCHED_LEARNED = 1,  /* pairs binned and ordered by the score predictor's output */
+  WFG_SCHED_GIVEN = 2,    /* the caller's order (wfg_set_order) */
+} wfg_sched_t;
+
+typedef struct {
+  double kernel_ms;       /* device time of the alignment kernels of the last wfg_run */
+  double pack_ms;         /* device time of the packing kernel */
+  double total_ms;        /* device time of the whole wfg_run (events on the context's stream) */
+  int launches;           /* kernels this library launched in the last wfg_run */
+  int retried_pairs;      /* pairs rerun with a larger arena after a scratch overflow */
+  int num_warps;          /* resident warps of the main launch */
+  int ring_w;             /* ring width (diagonals) of the main launch */
+  int64_t arena_bytes;    /* per-warp arena of the main launch */
+  int64_t total_runs;     /* CIGAR runs produced */
+  int64_t h2d_bytes, d2h_bytes; /* bytes copied by the last upload / fetch */
+} wfg_stats_t;
+
+wfg_context_t* wfg_context_create(int device);
+void wfg_context_destroy(wfg_context_t* ctx);
+/* Last error message of the context (empty string when none). */
+const char* wfg_last_error(wfg_context_t* ctx);
+
+/* Upload a batch from host memory: pattern i = seq[p_off[i] .. p_off[i]+plen[i]),
+ * text i = seq[t_off[i] .. t_off[i]+tlen[i]) of one host byte buffer of seq_len bytes.
+ * Copies to the device and leaves the batch resident until the next upload. */
+int wfg_upload(wfg_context_t* ctx, int num_pairs, const char* seq, int64_t seq_len,
+               const int64_t* p_off, const int* plen, const int64_t* t_off, const int* tlen);
+/* Processing order for WFG_SCHED_GIVEN (num_pairs indices, a permutation). */
+int wfg_set_order(wfg_context_t* ctx, const int* order);
+/* Predicted scores for WFG_SCHED_LEARNED (host array of num_pairs, WFA penalty units,
+ * e.g. from wfg_predict_scores). */
+int wfg_set_predictions(wfg_context_t* ctx, const float* predicted_scores);
+/* Align the resident batch on the device (pack + align); results stay on the device. */
+int wfg_run(wfg_context_t* ctx, const wfg_config_t* cfg, wfg_sched_t sched);
+/* Copy results of the last wfg_run to host arrays (any may be NULL). runs receives the
+ * dense run buffer (runs_cap entries at most); run_off/run_len index into it. */
+int wfg_fetch(wfg_context_t* ctx, int* scores, int* statuses, int64_t* run_off, int* run_len,
+              uint32_t* runs, int64_t runs_cap, int64_t* total_runs);
+/* Upload + run + fetch in one call (the end-to-end path). */
+int wfg_align_host(wfg_context_t* ctx, const wfg_config_t* cfg, wfg_sched_t sched,
+                   int num_pairs, const char* seq, int64_t seq_len,
+                   const int64_t* p_off, const int* plen, const int64_t* t_off, const int* tlen,
+                   int* scores, int* statuses, int64_t* run_off, int* run_len,
+                   uint32_t* runs, int64_t runs_cap, int64_t* total_runs);
+int wfg_get_stats(wfg_context_t* ctx, wfg_stats_t* stats);
+/* Write ~bytes of scratch to evict the L2 (between timed runs). */
+int wfg_flush_l2(wfg_context_t* ctx, int64_t bytes);
+/* Synchronize the context's stream. */
+int wfg_synchronize(wfg_context_t* ctx);
+
+/* Seeded synthetic pair generator (host; deterministic on every platform).
+ * workload: 1 = 1 kbp / 5 % (sub/ins/del 1/3 each, single-base indels),
+ *           2 = 150 bp / 2 %, 3 = uneven: log-uniform 100..10000 bp, 1..10 % error,
+ *           geometric indel length mean 2, 4 = long noisy: 50..100 kbp, 12 % error,
+ *           50/25/25 sub/ins/del, geometric indel length mean 3, 5 = equal mixture of 1..3.
+ * Two-phase: call with seq == NULL to get *seq_len_out (bytes needed), then again. */
+int wfg_generate(int workload, int num_pairs, uint64_t seed, char* seq, int64_t* seq_len_out,
+                 int64_t* p_off, int* plen, int64_t* t_off, int* tlen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WFA_GPU_H_ */

@@ -1,0 +1,133 @@
+"""ctypes access to the oracle builds (test infrastructure, never the product).
+
+  * libbiwfa_oracle.so  — the C restatement in biwfa_oracle.c (builds anywhere with gcc);
+  * libwfa2_ref.so      — the real WFA2-lib v2.3 compiled from the reference sources
+                          (only where the reference tree is mounted; see Makefile).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "_build" / "libbiwfa_oracle.so"
+REF_SO = HERE / "_ref" / "libwfa2_ref.so"
+WFA2_SRC = Path(os.environ.get("WFA2_SRC", "/root/reference/WFA2-lib"))
+
+
+class OrcResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("score", C.c_int), ("cigar_score", C.c_int), ("ops_len", C.c_int),
+                ("n_cells", C.c_int64), ("n_ext", C.c_int64), ("n_steps", C.c_int64),
+                ("max_leaf_score", C.c_int), ("max_depth", C.c_int)]
+
+
+def build_oracle() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
+    return ORACLE_SO
+
+
+def build_ref() -> Path | None:
+    """Builds the WFA2-lib reference library when its sources are present; else None."""
+    if not (WFA2_SRC / "wavefront" / "wavefront_align.c").exists():
+        return REF_SO if REF_SO.exists() else None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"WFA2={WFA2_SRC}"], check=True)
+    return REF_SO
+
+
+_orc = None
+_ref = None
+
+
+def oracle_lib() -> C.CDLL:
+    global _orc
+    if _orc is None:
+        if not ORACLE_SO.exists():
+            build_oracle()
+        lib = C.CDLL(str(ORACLE_SO))
+        lib.orc_biwfa_align.restype = C.c_int
+        lib.orc_biwfa_align.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_int, C.c_int, C.c_char_p, C.c_int, C.POINTER(OrcResult)]
+        lib.orc_biwfa_align_batch.restype = C.c_double
+        _orc = lib
+    return _orc
+
+
+def ref_lib() -> C.CDLL | None:
+    global _ref
+    if _ref is None:
+        if not REF_SO.exists():
+            return None
+        lib = C.CDLL(str(REF_SO))
+        lib.ref_biwfa_align.restype = C.c_int
+        _ref = lib
+    return _ref
+
+
+def _b(x) -> bytes:
+    return x.encode() if isinstance(x, str) else bytes(x)
+
+
+def rle(ops: str) -> str:
+    out, i = [], 0
+    while i < len(ops):
+        j = i
+        while j < len(ops) and ops[j] == ops[i]:
+            j += 1
+        out.append(f"{j - i}{ops[i]}")
+        i = j
+    return "".join(out)
+
+
+def oracle_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False):
+    """Returns (status, score, ops, OrcResult). score follows align_benchmark's printing:
+    the rescored CIGAR (full mode, -1 when the CIGAR is empty) or cigar->score (score-only)."""
+    p, t = _b(pattern), _b(text)
+    cap = len(p) + len(t) + 8
+    buf = C.create_string_buffer(cap)
+    r = OrcResult()
+    st = oracle_lib().orc_biwfa_align(p, len(p), t, len(t), *penalties, 1 if score_only else 0, buf, cap,
+                                      C.byref(r))
+    return st, r.score, buf.raw[:r.ops_len].decode(), r
+
+
+def ref_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False):
+    """The real WFA2-lib. Returns (status, printed score, ops, cigar->score) or None if unavailable."""
+    lib = ref_lib()
+    if lib is None:
+        return None
+    m, x, o, e = penalties
+    p, t = _b(pattern), _b(text)
+    cap = len(p) + len(t) + 8
+    buf = C.create_string_buffer(cap)
+    cs, rs, ol = C.c_int(), C.c_int(), C.c_int()
+    st = lib.ref_biwfa_align(p, len(p), t, len(t), m, x, o, e, 1 if score_only else 0, C.byref(cs), C.byref(rs),
+                             buf, cap, C.byref(ol))
+    ops = buf.raw[:ol.value].decode()
+    score = cs.value if score_only else (rs.value if ops else -1)
+    return st, score, ops, cs.value
+
+
+def oracle_batch_time(seq: np.ndarray, p_off, plen, t_off, tlen, penalties=(0, 4, 6, 2), score_only=False,
+                      threads: int = 1):
+    """Aligns a batch with the oracle on `threads` POSIX threads; returns (seconds, scores, status)."""
+    lib = oracle_lib()
+    n = int(len(plen))
+    p_off = np.ascontiguousarray(p_off, np.int64); t_off = np.ascontiguousarray(t_off, np.int64)
+    plen = np.ascontiguousarray(plen, np.int32); tlen = np.ascontiguousarray(tlen, np.int32)
+    ops_off = np.zeros(n, np.int64)
+    if n > 1:
+        ops_off[1:] = np.cumsum((plen.astype(np.int64) + tlen + 1))[:-1]
+    ops = np.empty(int((plen.astype(np.int64) + tlen + 1).sum()) + 1, np.uint8)
+    scores = np.empty(n, np.int32); status = np.empty(n, np.int32); ops_len = np.empty(n, np.int32)
+    i64p, ip = C.POINTER(C.c_int64), C.POINTER(C.c_int)
+    secs = lib.orc_biwfa_align_batch(
+        C.c_int(n), seq.ctypes.data_as(C.c_char_p), p_off.ctypes.data_as(i64p), plen.ctypes.data_as(ip),
+        seq.ctypes.data_as(C.c_char_p), t_off.ctypes.data_as(i64p), tlen.ctypes.data_as(ip),
+        C.c_int(penalties[0]), C.c_int(penalties[1]), C.c_int(penalties[2]), C.c_int(penalties[3]),
+        C.c_int(1 if score_only else 0), ops.ctypes.data_as(C.c_char_p), ops_off.ctypes.data_as(i64p),
+        scores.ctypes.data_as(ip), status.ctypes.data_as(ip), ops_len.ctypes.data_as(ip), C.c_int(threads))
+    return float(secs), scores, status

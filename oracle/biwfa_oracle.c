@@ -1,0 +1,709 @@
+/*
+ * TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT (see biwfa_oracle.h).
+ *
+ * Plain-C restatement of WFA2-lib v2.3 BiWFA, gap-affine, end-to-end, no heuristic.
+ * Every function names the WFA2-lib function (path:line, relative to WFA2-lib/) it
+ * restates. Semantics that matter for bit-exact CIGARs and are easy to lose:
+ *   - an absent or null input wavefront contributes lo = 1, hi = -1 to the output
+ *     limits (the shared null wavefront, wavefront/wavefront.c:110-140);
+ *   - reads outside [lo,hi] of a wavefront give OFFSET_NULL (init_ends,
+ *     wavefront/wavefront_compute.c:498-575);
+ *   - only M offsets are bounds-checked inside the recurrence; I/D keep
+ *     out-of-bounds interior values, only their ends are trimmed
+ *     (wavefront_compute_affine.c:65-85, wavefront_compute.c:579-613);
+ *   - the overlap scan order and strict "<" (wavefront_bialign.c:189-392);
+ *   - backtrace source priority via (offset<<4)|type with an UNSHIFTED null for
+ *     out-of-range sources (wavefront_backtrace.c:41-219, 320-529).
+ */
+#include "biwfa_oracle.h"
+
+#include <limits.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#define OFF_NULL (INT32_MIN / 2)            /* wavefront/wavefront_offset.h:45 */
+#define FALLBACK_MIN_SCORE 250              /* wavefront/wavefront_bialign.c:48 */
+#define FALLBACK_MIN_LENGTH 100             /* wavefront/wavefront_bialign.c:49 */
+#define RECOVERY_MIN_SCORE 500              /* wavefront/wavefront_bialign.c:50 */
+
+/* Internal statuses (wavefront/wfa.h:52-54) */
+#define ST_OK (-1)
+#define ST_END_REACHED (-2)
+#define ST_END_UNREACHABLE (-3)
+
+/* Components (alignment/affine2p_penalties.h:51-57) */
+enum { C_M = 0, C_I = 1, C_D = 3 };
+
+/* Backtrace types (wavefront/wavefront_backtrace.c:49-59) */
+enum { BT_M = 9, BT_D_EXT = 6, BT_D_OPEN = 5, BT_I_EXT = 2, BT_I_OPEN = 1 };
+
+/* ---------------------------------------------------------------- wavefronts */
+typedef struct {
+  int present;   /* the slot holds a wavefront (a non-NULL pointer in WFA2) */
+  int lo, hi;    /* effective range; lo > hi means null (trimmed empty) */
+  int base, cap; /* storage covers k in [base, base + cap) */
+  int32_t* off;
+} wf_t;
+
+static inline int wf_null(const wf_t* w) { return !w->present || w->lo > w->hi; }
+static inline int32_t wf_get(const wf_t* w, int k) {
+  return (w != NULL && w->present && w->lo <= k && k <= w->hi) ? w->off[k - w->base] : OFF_NULL;
+}
+static void wf_reserve(wf_t* w, int lo, int hi) {
+  if (w->off != NULL && lo >= w->base && hi < w->base + w->cap) return;
+  int len = hi - lo + 1;
+  int pad = len / 2 + 16;
+  free(w->off);
+  w->base = lo - pad;
+  w->cap = len + 2 * pad;
+  w->off = (int32_t*)malloc(sizeof(int32_t) * (size_t)w->cap);
+}
+
+typedef struct {
+  int x, o, e;        /* internal (possibly transformed) penalties */
+  int scope;          /* max_score_scope = max(o+e, x) + 1 (wavefront_components.c:81-93) */
+  int max_steps;      /* system.max_alignment_steps */
+} pen_t;
+
+typedef struct {
+  int64_t n_cells, n_ext, n_steps;
+  int max_leaf_score, max_depth;
+} counters_t;
+
+/* One direction of WFA over one window (a wavefront_aligner_t in WFA2). */
+typedef struct {
+  const pen_t* pen;
+  counters_t* cnt;
+  int modular;              /* ring of `scope` slots (score-only sub-aligners) or one slot per score */
+  int nslots;
+  wf_t* M; wf_t* I; wf_t* D;
+  const char* pat; const char* txt; /* oriented window */
+  int plen, tlen;
+  int comp_begin, comp_end;
+  int num_null_steps;
+  int status, status_score;
+  int end_k, end_off;
+} dir_t;
+
+static void dir_alloc(dir_t* d, const pen_t* pen, counters_t* cnt, int modular, int nslots) {
+  memset(d, 0, sizeof(*d));
+  d->pen = pen; d->cnt = cnt; d->modular = modular; d->nslots = nslots;
+  d->M = (wf_t*)calloc((size_t)nslots, sizeof(wf_t));
+  d->I = (wf_t*)calloc((size_t)nslots, sizeof(wf_t));
+  d->D = (wf_t*)calloc((size_t)nslots, sizeof(wf_t));
+}
+static void dir_grow(dir_t* d, int nslots) {
+  if (nslots <= d->nslots) return;
+  d->M = (wf_t*)realloc(d->M, sizeof(wf_t) * (size_t)nslots);
+  d->I = (wf_t*)realloc(d->I, sizeof(wf_t) * (size_t)nslots);
+  d->D = (wf_t*)realloc(d->D, sizeof(wf_t) * (size_t)nslots);
+  memset(d->M + d->nslots, 0, sizeof(wf_t) * (size_t)(nslots - d->nslots));
+  memset(d->I + d->nslots, 0, sizeof(wf_t) * (size_t)(nslots - d->nslots));
+  memset(d->D + d->nslots, 0, sizeof(wf_t) * (size_t)(nslots - d->nslots));
+  d->nslots = nslots;
+}
+static void dir_free(dir_t* d) {
+  for (int i = 0; i < d->nslots; ++i) { free(d->M[i].off); free(d->I[i].off); free(d->D[i].off); }
+  free(d->M); free(d->I); free(d->D);
+}
+static inline int dir_slot(const dir_t* d, int score) {
+  return d->modular ? score % d->pen->scope : score;
+}
+
+/* wavefront_aligner_init + init_wf (wavefront/wavefront_aligner.c:251-417) */
+static void dir_init(dir_t* d, const char* pat, int plen, const char* txt, int tlen, int cb, int ce) {
+  d->pat = pat; d->plen = plen; d->txt = txt; d->tlen = tlen;
+  d->comp_begin = cb; d->comp_end = ce;
+  d->num_null_steps = 0;
+  d->status = ST_OK; d->status_score = 0;
+  d->end_k = INT_MAX; d->end_off = OFF_NULL;
+  const int n = d->modular ? d->pen->scope : 1;
+  for (int i = 0; i < n && i < d->nslots; ++i) { d->M[i].present = d->I[i].present = d->D[i].present = 0; }
+  wf_t* w = (cb == C_M) ? &d->M[0] : (cb == C_I) ? &d->I[0] : &d->D[0];
+  wf_reserve(w, 0, 0);
+  w->present = 1; w->lo = 0; w->hi = 0; w->off[0 - w->base] = 0;
+}
+
+/* Fetch an input wavefront: NULL when score < 0, the slot is empty or the wavefront
+ * is null (wavefront_compute_get_*wavefront, wavefront/wavefront_compute.c:249-285). */
+static inline const wf_t* fetch(const dir_t* d, const wf_t* comp, int score) {
+  if (score < 0) return NULL;
+  int s = score;
+  if (d->modular && s > 0) s = s % d->pen->scope;
+  if (!d->modular && s >= d->nslots) return NULL;
+  const wf_t* w = &comp[s];
+  return wf_null(w) ? NULL : w;
+}
+
+/* Trim out-of-bounds ends (wavefront_compute_trim_ends, wavefront/wavefront_compute.c:579-613). */
+static void trim_ends(const dir_t* d, wf_t* w) {
+  const uint32_t tl = (uint32_t)d->tlen, pl = (uint32_t)d->plen;
+  int k;
+  for (k = w->hi; k >= w->lo; --k) {
+    const int32_t off = w->off[k - w->base];
+    if ((uint32_t)off <= tl && (uint32_t)(off - k) <= pl) break;
+  }
+  w->hi = k;
+  for (k = w->lo; k <= w->hi; ++k) {
+    const int32_t off = w->off[k - w->base];
+    if ((uint32_t)off <= tl && (uint32_t)(off - k) <= pl) break;
+  }
+  w->lo = k;
+}
+
+/* wavefront_compute_affine (wavefront/wavefront_compute_affine.c:229-260) with
+ * fetch_input (wavefront_compute.c:306-352), limits_input (:40-104),
+ * allocate_output(_null) (:382-494), the idm kernel (compute_affine.c:44-86)
+ * and process_ends (:614-632). */
+static void dir_compute(dir_t* d, int score) {
+  const pen_t* p = d->pen;
+  if (!d->modular && score >= d->nslots) dir_grow(d, score + 1 > 2 * d->nslots ? score + 1 : 2 * d->nslots);
+  const wf_t* mx = fetch(d, d->M, score - p->x);
+  const wf_t* mo = fetch(d, d->M, score - p->o - p->e);
+  const wf_t* ie = fetch(d, d->I, score - p->e);
+  const wf_t* de = fetch(d, d->D, score - p->e);
+  const int slot = dir_slot(d, score);
+  wf_t* om = &d->M[slot]; wf_t* oi = &d->I[slot]; wf_t* od = &d->D[slot];
+  d->cnt->n_steps++;
+  if (!mx && !mo && !ie && !de) {
+    d->num_null_steps++;
+    om->present = oi->present = od->present = 0;
+    return;
+  }
+  d->num_null_steps = 0;
+  /* Limits: a missing input is the shared null wavefront with lo=1, hi=-1. */
+  int lo = mx ? mx->lo : 1, hi = mx ? mx->hi : -1, t;
+  t = (mo ? mo->lo : 1) - 1; if (lo > t) lo = t;
+  t = (mo ? mo->hi : -1) + 1; if (hi < t) hi = t;
+  t = (ie ? ie->lo : 1) + 1; if (lo > t) lo = t;
+  t = (ie ? ie->hi : -1) + 1; if (hi < t) hi = t;
+  t = (de ? de->lo : 1) - 1; if (lo > t) lo = t;
+  t = (de ? de->hi : -1) - 1; if (hi < t) hi = t;
+  const int alloc_i = (mo != NULL) || (ie != NULL);
+  const int alloc_d = (mo != NULL) || (de != NULL);
+  wf_reserve(om, lo, hi); om->present = 1; om->lo = lo; om->hi = hi;
+  if (alloc_i) { wf_reserve(oi, lo, hi); oi->present = 1; oi->lo = lo; oi->hi = hi; } else oi->present = 0;
+  if (alloc_d) { wf_reserve(od, lo, hi); od->present = 1; od->lo = lo; od->hi = hi; } else od->present = 0;
+  d->cnt->n_cells += 3 * (int64_t)(hi - lo + 1);
+  const uint32_t tl = (uint32_t)d->tlen, pl = (uint32_t)d->plen;
+  for (int k = lo; k <= hi; ++k) {
+    const int32_t ins_o = wf_get(mo, k - 1), ins_e = wf_get(ie, k - 1);
+    const int32_t ins = (ins_o >= ins_e ? ins_o : ins_e) + 1;
+    const int32_t del_o = wf_get(mo, k + 1), del_e = wf_get(de, k + 1);
+    const int32_t del = (del_o >= del_e ? del_o : del_e);
+    const int32_t mis = wf_get(mx, k) + 1;
+    int32_t m = mis >= ins ? mis : ins;
+    m = del >= m ? del : m;
+    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = OFF_NULL;
+    if (alloc_i) oi->off[k - oi->base] = ins;
+    if (alloc_d) od->off[k - od->base] = del;
+    om->off[k - om->base] = m;
+  }
+  trim_ends(d, om);
+  if (alloc_i) trim_ends(d, oi);
+  if (alloc_d) trim_ends(d, od);
+}
+
+/* Longest common extension from (v, h): the sentinel comparison of
+ * wavefront_extend_matches_kernel_blockwise (wavefront_extend_kernels.c:68-92)
+ * written with explicit window bounds instead of EOS characters. */
+static inline int lcp(const char* P, int plen, const char* T, int tlen, int v, int h) {
+  int n = 0;
+  while (v + n + 8 <= plen && h + n + 8 <= tlen) {
+    uint64_t a, b;
+    memcpy(&a, P + v + n, 8); memcpy(&b, T + h + n, 8);
+    const uint64_t x = a ^ b;
+    if (x) return n + (__builtin_ctzll(x) >> 3);
+    n += 8;
+  }
+  while (v + n < plen && h + n < tlen && P[v + n] == T[h + n]) ++n;
+  return n;
+}
+
+/* wavefront_termination_end2end (wavefront/wavefront_termination.c:37-114) */
+static int termination(dir_t* d, int score) {
+  const int ak = d->tlen - d->plen;
+  const int aoff = d->tlen;
+  const int slot = dir_slot(d, score);
+  const wf_t* w = (d->comp_end == C_M) ? &d->M[slot] : (d->comp_end == C_I) ? &d->I[slot] : &d->D[slot];
+  if (!w->present || w->lo > ak || ak > w->hi) return 0;
+  if (w->off[ak - w->base] < aoff) return 0;
+  d->end_k = ak; d->end_off = aoff;
+  return 1;
+}
+
+/* wavefront_extend_end2end(_max) (wavefront/wavefront_extend.c:86-121, 173-211) */
+static int dir_extend(dir_t* d, int score, int* max_ak_out) {
+  if (max_ak_out) *max_ak_out = 0;
+  const int slot = dir_slot(d, score);
+  wf_t* m = &d->M[slot];
+  if (!m->present) {
+    if (d->num_null_steps > d->pen->scope) {
+      d->status = ST_END_UNREACHABLE; d->status_score = score; return 1;
+    }
+    return 0;
+  }
+  int max_ak = 0;
+  for (int k = m->lo; k <= m->hi; ++k) {
+    int32_t off = m->off[k - m->base];
+    if (off == OFF_NULL) continue;
+    const int n = lcp(d->pat, d->plen, d->txt, d->tlen, off - k, off);
+    d->cnt->n_ext += n + 1;
+    off += n;
+    m->off[k - m->base] = off;
+    const int ak = 2 * off - k;
+    if (max_ak < ak) max_ak = ak;
+  }
+  if (termination(d, score)) {
+    d->status = ST_END_REACHED; d->status_score = score; return 1;
+  }
+  if (max_ak_out) *max_ak_out = max_ak;
+  return 0;
+}
+
+/* ---------------------------------------------------------------- BiWFA */
+typedef struct {
+  int score, score_fwd, score_rev, k_fwd, k_rev, off_fwd, off_rev, comp;
+} bp_t; /* wf_bialign_breakpoint_t (wavefront/wavefront_bialigner.h:43-54) */
+
+typedef struct {
+  pen_t pen;
+  int match_orig, x_orig, o_orig, e_orig;
+  const char* P; const char* T; /* forward full sequences */
+  char* rP; char* rT;           /* reversed full sequences */
+  int plen_full, tlen_full;
+  dir_t fwd, rev, base;
+  char* ops; int ops_len, ops_cap;
+  char* leaf;                   /* leaf backtrace buffer (written backwards) */
+  int leaf_cap;
+  int cigar_score;
+  counters_t cnt;
+} ctx_t;
+
+/* wavefront_bialign_breakpoint_indel2indel (wavefront/wavefront_bialign.c:189-256) */
+static void bp_indel(const ctx_t* c, int plen, int tlen, int fwd, int s0, int s1,
+                     const wf_t* w0, const wf_t* w1, int comp, bp_t* bp) {
+  const int go = c->pen.o;
+  const int lo0 = w0->lo, hi0 = w0->hi;
+  const int lo1 = tlen - plen - w1->hi, hi1 = tlen - plen - w1->lo;
+  if (hi1 < lo0 || hi0 < lo1) return;
+  const int min_hi = hi0 < hi1 ? hi0 : hi1;
+  const int max_lo = lo0 > lo1 ? lo0 : lo1;
+  for (int k0 = max_lo; k0 <= min_hi; ++k0) {
+    const int k1 = tlen - plen - k0;
+    const int32_t d0 = w0->off[k0 - w0->base], d1 = w1->off[k1 - w1->base];
+    if (d0 + d1 >= tlen && s0 + s1 - go < bp->score) {
+      if (fwd) {
+        const int v = d0 - k0, h = d0;
+        if (v > plen || h > tlen) continue;
+        bp->score_fwd = s0; bp->score_rev = s1; bp->k_fwd = k0; bp->k_rev = k1;
+        bp->off_fwd = d0; bp->off_rev = d1;
+      } else {
+        const int v = d1 - k1, h = d1;
+        if (v > plen || h > tlen) continue;
+        bp->score_fwd = s1; bp->score_rev = s0; bp->k_fwd = k1; bp->k_rev = k0;
+        bp->off_fwd = d1; bp->off_rev = d0;
+      }
+      bp->score = s0 + s1 - go;
+      bp->comp = comp;
+      return;
+    }
+  }
+}
+
+/* wavefront_bialign_breakpoint_m2m (wavefront/wavefront_bialign.c:257-310) */
+static void bp_m2m(int plen, int tlen, int fwd, int s0, int s1,
+                   const wf_t* w0, const wf_t* w1, bp_t* bp) {
+  const int lo0 = w0->lo, hi0 = w0->hi;
+  const int lo1 = tlen - plen - w1->hi, hi1 = tlen - plen - w1->lo;
+  if (hi1 < lo0 || hi0 < lo1) return;
+  const int min_hi = hi0 < hi1 ? hi0 : hi1;
+  const int max_lo = lo0 > lo1 ? lo0 : lo1;
+  for (int k0 = max_lo; k0 <= min_hi; ++k0) {
+    const int k1 = tlen - plen - k0;
+    const int32_t m0 = w0->off[k0 - w0->base], m1 = w1->off[k1 - w1->base];
+    if (m0 + m1 >= tlen && s0 + s1 < bp->score) {
+      if (fwd) {
+        bp->score_fwd = s0; bp->score_rev = s1; bp->k_fwd = k0; bp->k_rev = k1;
+        bp->off_fwd = m0; bp->off_rev = m1;
+      } else {
+        bp->score_fwd = s1; bp->score_rev = s0; bp->k_fwd = k1; bp->k_rev = k0;
+        bp->off_fwd = m1; bp->off_rev = m0;
+      }
+      bp->score = s0 + s1;
+      bp->comp = C_M;
+      return;
+    }
+  }
+}
+
+/* wavefront_bialign_overlap (wavefront/wavefront_bialign.c:314-392), gap-affine */
+static void overlap(const ctx_t* c, const dir_t* d0, const dir_t* d1, int s0, int s1, int fwd, bp_t* bp) {
+  const int scope = c->pen.scope, go = c->pen.o;
+  const int plen = d0->plen, tlen = d0->tlen;
+  const int sm0 = s0 % scope;
+  const wf_t* m0 = &d0->M[sm0];
+  if (!m0->present) return;
+  const wf_t* dd0 = &d0->D[sm0];
+  const wf_t* ii0 = &d0->I[sm0];
+  for (int i = 0; i < scope; ++i) {
+    const int si = s1 - i;
+    if (si < 0) break;
+    const int smi = si % scope;
+    if (s0 + si - go >= bp->score) continue;
+    const wf_t* dd1 = &d1->D[smi];
+    if (dd0->present && dd1->present) bp_indel(c, plen, tlen, fwd, s0, si, dd0, dd1, C_D, bp);
+    const wf_t* ii1 = &d1->I[smi];
+    if (ii0->present && ii1->present) bp_indel(c, plen, tlen, fwd, s0, si, ii0, ii1, C_I, bp);
+    if (s0 + si >= bp->score) continue;
+    const wf_t* mm1 = &d1->M[smi];
+    if (mm1->present) bp_m2m(plen, tlen, fwd, s0, si, m0, mm1, bp);
+  }
+}
+
+/* Window set-up: wavefront_bialigner_set_sequences_bounds (wavefront_bialigner.c:107-121)
+ * and wavefront_sequences_set_bounds (wavefront_sequences.c:274-309). */
+static void set_windows(ctx_t* c, int pb, int pe, int tb, int te, int cb, int ce) {
+  dir_init(&c->fwd, c->P + pb, pe - pb, c->T + tb, te - tb, cb, ce);
+  dir_init(&c->rev, c->rP + (c->plen_full - pe), pe - pb, c->rT + (c->tlen_full - te), te - tb, ce, cb);
+}
+
+/* wavefront_bialign_find_breakpoint (wavefront/wavefront_bialign.c:411-519) */
+static int find_breakpoint(ctx_t* c, int pb, int pe, int tb, int te, int cb, int ce, bp_t* bp) {
+  dir_t* F = &c->fwd; dir_t* R = &c->rev;
+  set_windows(c, pb, pe, tb, te, cb, ce);
+  const int plen = pe - pb, tlen = te - tb;
+  const int max_steps = c->pen.max_steps;
+  const int max_antidiag = plen + tlen - 1;
+  int sf = 0, sr = 0, fmax = 0, rmax = 0, ak;
+  bp->score = INT_MAX;
+  if (dir_extend(F, sf, &fmax)) return F->status;
+  if (dir_extend(R, sr, &rmax)) return R->status;
+  int last_fwd = 0;
+  for (;;) {
+    if (fmax + rmax >= max_antidiag) break;
+    ++sf; dir_compute(F, sf);
+    const int qf = dir_extend(F, sf, &ak);
+    if (fmax < ak) fmax = ak;
+    last_fwd = 1;
+    if (qf) return F->status;
+    if (fmax + rmax >= max_antidiag) break;
+    ++sr; dir_compute(R, sr);
+    const int qr = dir_extend(R, sr, &ak);
+    if (rmax < ak) rmax = ak;
+    last_fwd = 0;
+    if (qr) return R->status;
+    if (sr + sf >= max_steps) return ORC_STATUS_MAX_STEPS_REACHED;
+  }
+  const int scope = c->pen.scope, go = c->pen.o;
+  for (;;) {
+    if (last_fwd) {
+      const int min_sr = (sr > scope - 1) ? sr - (scope - 1) : 0;
+      if (sf + min_sr - go >= bp->score) break;
+      overlap(c, F, R, sf, sr, 1, bp);
+      ++sr; dir_compute(R, sr);
+      if (dir_extend(R, sr, NULL)) return R->status;
+    }
+    const int min_sf = (sf > scope - 1) ? sf - (scope - 1) : 0;
+    if (min_sf + sr - go >= bp->score) break;
+    overlap(c, R, F, sr, sf, 0, bp);
+    ++sf; dir_compute(F, sf);
+    if (dir_extend(F, sf, NULL)) return F->status;
+    if (sr + sf >= max_steps) return ORC_STATUS_MAX_STEPS_REACHED;
+    last_fwd = 1;
+  }
+  return ST_OK;
+}
+
+/* Backtrace source fetchers (wavefront/wavefront_backtrace.c:64-219). An absent or
+ * out-of-range source is the UNSHIFTED null; an in-range source is (offset<<4)|type. */
+static inline int64_t bt_src(const dir_t* d, const wf_t* comp, int score, int kk, int add, int type) {
+  if (score < 0 || score >= d->nslots) return OFF_NULL;
+  const wf_t* w = &comp[score];
+  if (w->present && w->lo <= kk && kk <= w->hi) {
+    return (int64_t)((uint64_t)(int64_t)(w->off[kk - w->base] + add) << 4) | type;
+  }
+  return OFF_NULL;
+}
+static inline int64_t max64(int64_t a, int64_t b) { return a >= b ? a : b; }
+
+/* wavefront_backtrace_affine (wavefront/wavefront_backtrace.c:320-529), gap-affine.
+ * Writes the ops of the leaf into c->leaf backwards; returns the first index. */
+static int backtrace_affine(ctx_t* c, const dir_t* d, int score_end, int k, int32_t off) {
+  const pen_t* p = &c->pen;
+  char* ops = c->leaf;
+  int pos = c->leaf_cap - 1; /* next write position (backwards) */
+  int matrix = d->comp_end;
+  int score = score_end;
+  int h = off, v = off - k;
+  if (d->comp_end == C_M) {
+    if (v < d->plen) { for (int i = d->plen - v; i > 0; --i) ops[pos--] = 'D'; }
+    if (h < d->tlen) { for (int i = d->tlen - h; i > 0; --i) ops[pos--] = 'I'; }
+  }
+  while (v > 0 && h > 0 && score > 0) {
+    const int mm = score - p->x, go = score - p->o - p->e, ge = score - p->e;
+    int64_t max_all;
+    if (matrix == C_M) {
+      const int64_t mis = bt_src(d, d->M, mm, k, 1, BT_M);
+      const int64_t io = bt_src(d, d->M, go, k - 1, 1, BT_I_OPEN);
+      const int64_t ix = bt_src(d, d->I, ge, k - 1, 1, BT_I_EXT);
+      const int64_t dop = bt_src(d, d->M, go, k + 1, 0, BT_D_OPEN);
+      const int64_t dx = bt_src(d, d->D, ge, k + 1, 0, BT_D_EXT);
+      max_all = max64(mis, max64(max64(io, ix), max64(dop, dx)));
+    } else if (matrix == C_I) {
+      max_all = max64(bt_src(d, d->M, go, k - 1, 1, BT_I_OPEN), bt_src(d, d->I, ge, k - 1, 1, BT_I_EXT));
+    } else {
+      max_all = max64(bt_src(d, d->M, go, k + 1, 0, BT_D_OPEN), bt_src(d, d->D, ge, k + 1, 0, BT_D_EXT));
+    }
+    if (max_all < 0) break;
+    if (matrix == C_M) {
+      const int max_off = (int)(max_all >> 4);
+      const int nm = off - max_off;
+      for (int i = 0; i < nm; ++i) ops[pos--] = 'M';
+      off = max_off;
+      v = off - k; h = off;
+      if (v <= 0 || h <= 0) break;
+    }
+    const int type = (int)(max_all & 0xF);
+    switch (type) {
+      case BT_M: score = mm; matrix = C_M; break;
+      case BT_I_OPEN: score = go; matrix = C_M; break;
+      case BT_I_EXT: score = ge; matrix = C_I; break;
+      case BT_D_OPEN: score = go; matrix = C_M; break;
+      default: score = ge; matrix = C_D; break; /* BT_D_EXT */
+    }
+    if (type == BT_M) { ops[pos--] = 'X'; --off; }
+    else if (type == BT_I_OPEN || type == BT_I_EXT) { ops[pos--] = 'I'; --k; --off; }
+    else { ops[pos--] = 'D'; ++k; }
+    v = off - k; h = off;
+  }
+  if (matrix == C_M) {
+    if (v > 0 && h > 0) {
+      const int nm = v < h ? v : h;
+      for (int i = 0; i < nm; ++i) ops[pos--] = 'M';
+      v -= nm; h -= nm;
+    }
+    while (v > 0) { ops[pos--] = 'D'; --v; }
+    while (h > 0) { ops[pos--] = 'I'; --h; }
+  }
+  return pos + 1;
+}
+
+static void append_ops(ctx_t* c, const char* src, int n) {
+  if (c->ops != NULL && c->ops_len + n <= c->ops_cap) memcpy(c->ops + c->ops_len, src, (size_t)n);
+  c->ops_len += n;
+}
+static void append_run(ctx_t* c, char op, int n) {
+  for (int i = 0; i < n; ++i) {
+    if (c->ops != NULL && c->ops_len < c->ops_cap) c->ops[c->ops_len] = op;
+    c->ops_len++;
+  }
+}
+
+/* wavefront_bialign_base (wavefront/wavefront_bialign.c:155-185) ->
+ * wavefront_unialign_init / wavefront_unialign / wavefront_unialign_terminate
+ * (wavefront/wavefront_unialign.c:54-94, 147-273). */
+static int bialign_base(ctx_t* c, int pb, int pe, int tb, int te, int cb, int ce) {
+  dir_t* B = &c->base;
+  dir_init(B, c->P + pb, pe - pb, c->T + tb, te - tb, cb, ce);
+  int score = 0;
+  for (;;) {
+    if (dir_extend(B, score, NULL)) break;
+    ++score;
+    dir_compute(B, score);
+    if (score >= c->pen.max_steps) return ORC_STATUS_UNATTAINABLE;
+  }
+  if (c->cnt.max_leaf_score < score) c->cnt.max_leaf_score = score;
+  if (B->status != ST_END_REACHED) return ORC_STATUS_UNATTAINABLE;
+  const int need = 2 * (B->plen + B->tlen) + 8;
+  if (c->leaf_cap < need) { free(c->leaf); c->leaf_cap = need; c->leaf = (char*)malloc((size_t)need); }
+  if (B->end_off != OFF_NULL) {
+    const int first = backtrace_affine(c, B, score, B->end_k, B->end_off);
+    append_ops(c, c->leaf + first, c->leaf_cap - first);
+  }
+  return ST_OK;
+}
+
+static int classic_score(const ctx_t* c, int plen, int tlen, int wf_score) {
+  /* wavefront_compute_classic_score (wavefront/wavefront_compute.c:108-120) */
+  const int swg_match = -c->match_orig;
+  if (swg_match == 0) return -wf_score;
+  return (swg_match * (plen + tlen) - wf_score) / 2; /* WF_SCORE_TO_SW_SCORE */
+}
+
+/* wavefront_bialign_alignment (wavefront/wavefront_bialign.c:581-658) */
+static int bialign_alignment(ctx_t* c, int pb, int pe, int tb, int te, int cb, int ce, int rem, int level) {
+  const int plen = pe - pb, tlen = te - tb;
+  if (c->cnt.max_depth < level) c->cnt.max_depth = level;
+  if (tlen == 0) { append_run(c, 'D', plen); return ST_OK; }
+  if (plen == 0) { append_run(c, 'I', tlen); return ST_OK; }
+  if (rem <= FALLBACK_MIN_SCORE) return bialign_base(c, pb, pe, tb, te, cb, ce);
+  bp_t bp;
+  int st = find_breakpoint(c, pb, pe, tb, te, cb, ce, &bp);
+  if (st != ST_OK) {
+    /* wavefront_bialign_find_breakpoint_exception (:520-547) */
+    if (st == ST_END_REACHED) {
+      const int reached = (c->fwd.status == ST_END_REACHED) ? c->fwd.status_score : c->rev.status_score;
+      if (reached <= RECOVERY_MIN_SCORE) return bialign_base(c, pb, pe, tb, te, cb, ce);
+      return ST_END_UNREACHABLE;
+    }
+    return st;
+  }
+  const int bh = bp.off_fwd, bv = bp.off_fwd - bp.k_fwd;
+  st = bialign_alignment(c, pb, pb + bv, tb, tb + bh, cb, bp.comp, bp.score_fwd, level + 1);
+  if (st != ST_OK) return st;
+  st = bialign_alignment(c, pb + bv, pe, tb + bh, te, bp.comp, ce, bp.score_rev, level + 1);
+  if (st != ST_OK) return st;
+  if (level == 0) c->cigar_score = classic_score(c, plen, tlen, bp.score);
+  return ST_OK;
+}
+
+/* cigar_score_gap_affine (alignment/cigar.c:277-303) with the caller's penalties. */
+static int rescore(const char* ops, int n, int match, int x, int o, int e) {
+  char last = 0; int score = 0;
+  for (int i = 0; i < n; ++i) {
+    switch (ops[i]) {
+      case 'M': score -= match; break;
+      case 'X': score -= x; break;
+      case 'D': score -= e + (last == 'D' ? 0 : o); break;
+      case 'I': score -= e + (last == 'I' ? 0 : o); break;
+      default: break;
+    }
+    last = ops[i];
+  }
+  return score;
+}
+
+static void ctx_init(ctx_t* c, int match, int x, int o, int e) {
+  memset(c, 0, sizeof(*c));
+  c->match_orig = match; c->x_orig = x; c->o_orig = o; c->e_orig = e;
+  /* wavefront_penalties_set_affine (wavefront/wavefront_penalties.c:95-130) */
+  if (match < 0) {
+    c->pen.x = 2 * x - 2 * match; c->pen.o = 2 * o; c->pen.e = 2 * e - match;
+  } else {
+    c->pen.x = x; c->pen.o = o; c->pen.e = e;
+  }
+  const int oe = c->pen.o + c->pen.e;
+  c->pen.scope = (oe > c->pen.x ? oe : c->pen.x) + 1;
+  c->pen.max_steps = INT_MAX;
+  c->cnt.max_leaf_score = -1;
+  dir_alloc(&c->fwd, &c->pen, &c->cnt, 1, c->pen.scope);
+  dir_alloc(&c->rev, &c->pen, &c->cnt, 1, c->pen.scope);
+  dir_alloc(&c->base, &c->pen, &c->cnt, 0, 64);
+}
+static void ctx_free(ctx_t* c) {
+  dir_free(&c->fwd); dir_free(&c->rev); dir_free(&c->base);
+  free(c->rP); free(c->rT); free(c->leaf);
+}
+
+static int validate(int match, int x, int o, int e) {
+  return !(match > 0 || x <= 0 || o < 0 || e <= 0);
+}
+
+static int align_one(ctx_t* c, const char* pattern, int plen, const char* text, int tlen,
+                     int score_only, char* ops, int ops_cap, orc_result_t* res) {
+  c->P = pattern; c->T = text; c->plen_full = plen; c->tlen_full = tlen;
+  c->rP = (char*)realloc(c->rP, (size_t)plen + 1);
+  c->rT = (char*)realloc(c->rT, (size_t)tlen + 1);
+  for (int i = 0; i < plen; ++i) c->rP[i] = pattern[plen - 1 - i];
+  for (int i = 0; i < tlen; ++i) c->rT[i] = text[tlen - 1 - i];
+  c->ops = ops; c->ops_cap = ops_cap; c->ops_len = 0;
+  c->cigar_score = INT32_MIN;
+  memset(&c->cnt, 0, sizeof(c->cnt));
+  c->cnt.max_leaf_score = -1;
+  int st, final_status;
+  if (score_only) {
+    /* wavefront_bialign_compute_score (wavefront/wavefront_bialign.c:662-699) */
+    bp_t bp;
+    st = find_breakpoint(c, 0, plen, 0, tlen, C_M, C_M, &bp);
+    if (st == ST_OK || st == ST_END_REACHED) {
+      if (st == ST_END_REACHED)
+        bp.score = (c->fwd.status == ST_END_REACHED) ? c->fwd.status_score : c->rev.status_score;
+      c->cigar_score = classic_score(c, plen, tlen, bp.score);
+      st = ST_OK;
+    }
+  } else {
+    /* wavefront_bialign (wavefront/wavefront_bialign.c:703-730) */
+    const int min_len = (plen > tlen ? plen : tlen) <= FALLBACK_MIN_LENGTH;
+    st = bialign_alignment(c, 0, plen, 0, tlen, C_M, C_M, min_len ? 0 : INT_MAX, 0);
+  }
+  if (st == ST_OK) final_status = ORC_STATUS_ALG_COMPLETED;
+  else if (st == ORC_STATUS_MAX_STEPS_REACHED || st == ORC_STATUS_OOM) final_status = st;
+  else final_status = ORC_STATUS_UNATTAINABLE;
+  if (res) {
+    res->status = final_status;
+    res->cigar_score = c->cigar_score;
+    res->ops_len = score_only ? 0 : c->ops_len;
+    if (score_only) res->score = c->cigar_score;
+    else res->score = (c->ops_len > 0 && c->ops_len <= ops_cap)
+        ? rescore(ops, c->ops_len, c->match_orig, c->x_orig, c->o_orig, c->e_orig) : -1;
+    res->n_cells = c->cnt.n_cells; res->n_ext = c->cnt.n_ext; res->n_steps = c->cnt.n_steps;
+    res->max_leaf_score = c->cnt.max_leaf_score; res->max_depth = c->cnt.max_depth;
+  }
+  return final_status;
+}
+
+int orc_biwfa_align(const char* pattern, int plen, const char* text, int tlen,
+                    int match, int mismatch, int gap_open, int gap_ext,
+                    int score_only, char* ops, int ops_cap, orc_result_t* res) {
+  if (!validate(match, mismatch, gap_open, gap_ext) || plen < 0 || tlen < 0) {
+    if (res) { memset(res, 0, sizeof(*res)); res->status = ORC_STATUS_UNATTAINABLE; res->score = -1; }
+    return ORC_STATUS_UNATTAINABLE;
+  }
+  ctx_t c;
+  ctx_init(&c, match, mismatch, gap_open, gap_ext);
+  const int st = align_one(&c, pattern, plen, text, tlen, score_only, ops, ops_cap, res);
+  ctx_free(&c);
+  return st;
+}
+
+/* ---------------------------------------------------------------- batch (CPU baseline) */
+typedef struct {
+  int tid, nthreads, n;
+  const char* pat; const int64_t* pat_off; const int* plen;
+  const char* txt; const int64_t* txt_off; const int* tlen;
+  int match, x, o, e, score_only;
+  char* ops; const int64_t* ops_off;
+  int* scores; int* status; int* ops_len;
+} job_t;
+
+static void* batch_worker(void* arg) {
+  job_t* j = (job_t*)arg;
+  ctx_t c;
+  ctx_init(&c, j->match, j->x, j->o, j->e);
+  for (int i = j->tid; i < j->n; i += j->nthreads) {
+    orc_result_t r;
+    const int cap = j->plen[i] + j->tlen[i] + 1;
+    char* ops = j->score_only ? NULL : j->ops + j->ops_off[i];
+    align_one(&c, j->pat + j->pat_off[i], j->plen[i], j->txt + j->txt_off[i], j->tlen[i],
+              j->score_only, ops, cap, &r);
+    j->scores[i] = r.score; j->status[i] = r.status; j->ops_len[i] = r.ops_len;
+  }
+  ctx_free(&c);
+  return NULL;
+}
+
+double orc_biwfa_align_batch(int n, const char* pat, const int64_t* pat_off, const int* plen,
+                             const char* txt, const int64_t* txt_off, const int* tlen,
+                             int match, int mismatch, int gap_open, int gap_ext, int score_only,
+                             char* ops, const int64_t* ops_off,
+                             int* scores, int* status, int* ops_len, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (!validate(match, mismatch, gap_open, gap_ext)) return -1.0;
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+  job_t* jobs = (job_t*)malloc(sizeof(job_t) * (size_t)nthreads);
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  for (int t = 0; t < nthreads; ++t) {
+    job_t j = {t, nthreads, n, pat, pat_off, plen, txt, txt_off, tlen, match, mismatch, gap_open, gap_ext,
+               score_only, ops, ops_off, scores, status, ops_len};
+    jobs[t] = j;
+    pthread_create(&th[t], NULL, batch_worker, &jobs[t]);
+  }
+  for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  free(th); free(jobs);
+  return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}

@@ -1,0 +1,54 @@
+/*
+ * Test infrastructure only: a thin shim over the real WFA2-lib v2.3 API, compiled
+ * together with the WFA2-lib sources into oracle/_ref/libwfa2_ref.so. It is used to
+ * pin the C restatement in oracle/biwfa_oracle.c and to generate golden fixtures.
+ * Nothing in the product links or calls it.
+ *
+ * The attribute set is the exact BiWFA configuration of the hot path:
+ *   distance_metric = gap_affine, penalties {match, x, o, e},
+ *   memory_mode = wavefront_memory_ultralow, heuristic = wf_heuristic_none,
+ *   alignment_scope = compute_alignment (or compute_score).
+ * This is the configuration align_benchmark uses for
+ * `-a gap-affine-wfa --wfa-memory=ultralow` (tools/align_benchmark/align_benchmark.c:155-241).
+ */
+#include <string.h>
+#include "wavefront/wavefront_align.h"
+#include "alignment/cigar.h"
+
+/* Returns the WFA2 status. On success writes:
+ *   *cigar_score_out : wf_aligner->cigar->score as WFA2 leaves it
+ *   *rescore_out     : cigar_score_gap_affine() of the ops (what align_benchmark prints)
+ *   ops_out[0..*ops_len) : raw operations (M/X/I/D)
+ * ops_cap must be >= plen + tlen + 1. */
+int ref_biwfa_align(const char* pattern, int plen, const char* text, int tlen,
+                    int match, int mismatch, int gap_open, int gap_ext, int score_only,
+                    int* cigar_score_out, int* rescore_out,
+                    char* ops_out, int ops_cap, int* ops_len) {
+  wavefront_aligner_attr_t attr = wavefront_aligner_attr_default;
+  attr.distance_metric = gap_affine;
+  attr.affine_penalties.match = match;
+  attr.affine_penalties.mismatch = mismatch;
+  attr.affine_penalties.gap_opening = gap_open;
+  attr.affine_penalties.gap_extension = gap_ext;
+  attr.memory_mode = wavefront_memory_ultralow;
+  attr.heuristic.strategy = wf_heuristic_none;
+  attr.alignment_scope = score_only ? compute_score : compute_alignment;
+  wavefront_aligner_t* const wf = wavefront_aligner_new(&attr);
+  const int status = wavefront_align(wf, pattern, plen, text, tlen);
+  cigar_t* const cigar = wf->cigar;
+  *cigar_score_out = cigar->score;
+  *ops_len = 0;
+  *rescore_out = -1;
+  if (!score_only && cigar->begin_offset < cigar->end_offset) {
+    const int n = cigar->end_offset - cigar->begin_offset;
+    if (n < ops_cap) {
+      memcpy(ops_out, cigar->operations + cigar->begin_offset, n);
+      ops_out[n] = '\0';
+      *ops_len = n;
+    }
+    affine_penalties_t pen = {match, mismatch, gap_open, gap_ext};
+    *rescore_out = cigar_score_gap_affine(cigar, &pen);
+  }
+  wavefront_aligner_delete(wf);
+  return status;
+}

@@ -1,0 +1,126 @@
+"""Regenerates the golden fixtures in this folder (run where the reference tree is mounted).
+
+1. wfa2_utest.json.gz — WFA2-lib's own test vectors for this path, read as text from
+   WFA2-lib/tests/: the 305 input pairs (wfa.utest.seq) and the expected `score\\tCIGAR`
+   lines of the BiWFA gap-affine runs (test.biwfa.affine{,.p0..p5}.alg) and the BiWFA
+   score-only runs (test.biwfa.score.affine{,.p0..p5}.alg). Penalties per file follow
+   WFA2-lib/tests/wfa.utest.sh:47-59.
+2. wfa2_ref_cases.json.gz — outputs of the real WFA2-lib v2.3 (oracle/_ref/libwfa2_ref.so,
+   compiled from the reference sources by oracle/Makefile) on seeded synthetic pairs of
+   every workload and on edge cases, so the GPU tests can pin parity on the GPU machine where
+   the reference is absent.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import gzip
+import json
+import random
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+WFA2_TESTS = Path("/root/reference/WFA2-lib/tests")
+
+UTEST_SETS = {
+    # name: (penalties (match, mismatch, gap_open, gap_ext), score_only)
+    "test.biwfa.affine.alg": ((0, 4, 6, 2), False),
+    "test.biwfa.affine.p0.alg": ((0, 1, 2, 1), False),
+    "test.biwfa.affine.p1.alg": ((0, 3, 1, 4), False),
+    "test.biwfa.affine.p2.alg": ((0, 5, 3, 2), False),
+    "test.biwfa.affine.p3.alg": ((-5, 1, 2, 1), False),
+    "test.biwfa.affine.p4.alg": ((-2, 3, 1, 4), False),
+    "test.biwfa.affine.p5.alg": ((-3, 5, 3, 2), False),
+    "test.biwfa.score.affine.alg": ((0, 4, 6, 2), True),
+    "test.biwfa.score.affine.p0.alg": ((0, 1, 2, 1), True),
+    "test.biwfa.score.affine.p1.alg": ((0, 3, 1, 4), True),
+    "test.biwfa.score.affine.p2.alg": ((0, 5, 3, 2), True),
+    "test.biwfa.score.affine.p3.alg": ((-5, 1, 2, 1), True),
+    "test.biwfa.score.affine.p4.alg": ((-2, 3, 1, 4), True),
+    "test.biwfa.score.affine.p5.alg": ((-3, 5, 3, 2), True),
+}
+
+
+def read_seq_file(path: Path):
+    lines = path.read_text().split("\n")
+    pairs = []
+    for i in range(0, len(lines) - 1, 2):
+        if lines[i].startswith(">") and lines[i + 1].startswith("<"):
+            pairs.append((lines[i][1:], lines[i + 1][1:]))
+    return pairs
+
+
+def make_utest():
+    pairs = read_seq_file(WFA2_TESTS / "wfa.utest.seq")
+    sets = {}
+    for name, (pen, score_only) in UTEST_SETS.items():
+        lines = (WFA2_TESTS / "wfa.utest.check" / name).read_text().split("\n")[: len(pairs)]
+        sets[name] = {"penalties": list(pen), "score_only": score_only, "lines": lines}
+    out = {"source": "WFA2-lib/tests (v2.3)", "pairs": pairs, "sets": sets}
+    with gzip.open(HERE / "wfa2_utest.json.gz", "wt") as f:
+        json.dump(out, f)
+    print(f"wfa2_utest.json.gz: {len(pairs)} pairs x {len(sets)} sets")
+
+
+def edge_pairs():
+    rnd = random.Random(2024)
+
+    def rs(n, alphabet="ACGT"):
+        return "".join(rnd.choice(alphabet) for _ in range(n))
+
+    a150, b150 = rs(150), rs(150)
+    a100, b100 = rs(100), rs(100)
+    a101, b101 = rs(101), rs(101)
+    rep = "ACGTTG" * 60
+    return [
+        ("", ""), ("", "ACGT"), ("ACGT", ""), ("A", "A"), ("A", "C"), ("A", ""), ("", "G"),
+        ("ACGT" * 50, "ACGT" * 50), (a150, b150), (a100, b100), (a101, b101),
+        (rs(10), rs(1000)), (rs(1000), rs(10)), (rs(300), rs(300)),
+        ("ACGTNNNNACGTACGTNACGT" * 6, "ACGTNNACGTACGTTNACGT" * 6),
+        ("acgtACGTacgt" * 12, "ACGTACGTacgt" * 12),
+        ("A" * 400, "A" * 380 + "C" * 20), ("A" * 200, "A" * 230),
+        (rep, rep[:150] + "TTTT" + rep[150:]), (rep, rep[:100] + rep[130:]),
+        ("GATTACA" * 30, "GATCACA" * 30), (rs(5000, "AC"), rs(5000, "AC")),
+    ]
+
+
+def make_ref_cases():
+    import biwfa_gpu_pii2025_gb300 as pkg
+    from oracle import binding
+    if binding.build_ref() is None:
+        raise SystemExit("oracle/_ref cannot be built: WFA2-lib sources not found")
+    cases = []
+
+    def add(tag, pen, score_only, pairs):
+        rows = []
+        for p, t in pairs:
+            st, score, ops, cs = binding.ref_align(p, t, pen, score_only)
+            rows.append([p, t, st, score, binding.rle(ops) if ops else "-"])
+        cases.append({"tag": tag, "penalties": list(pen), "score_only": score_only, "pairs": rows})
+        print(f"  {tag}: {len(rows)} pairs")
+
+    def gen(workload, n, seed):
+        b = pkg.PairBatch.generate(workload, n, seed)
+        return [(b.pattern(i).decode(), b.text(i).decode()) for i in range(b.n)]
+
+    add("w1_1kbp_5pct", (0, 4, 6, 2), False, gen(1, 24, 101))
+    add("w2_150bp_2pct", (0, 4, 6, 2), False, gen(2, 96, 102))
+    add("w3_uneven", (0, 4, 6, 2), False, gen(3, 24, 103))
+    add("w4_long_noisy", (0, 4, 6, 2), False, gen(4, 1, 104))
+    add("w5_mixture_score_only", (0, 4, 6, 2), True, gen(5, 48, 105))
+    edges = edge_pairs()
+    for pen in [(0, 4, 6, 2), (0, 1, 2, 1), (0, 3, 1, 4), (0, 5, 3, 2), (-5, 1, 2, 1), (-2, 3, 1, 4)]:
+        add(f"edge_{'_'.join(map(str, pen))}", pen, False, edges)
+    add("edge_score_only", (0, 4, 6, 2), True, edges)
+    with gzip.open(HERE / "wfa2_ref_cases.json.gz", "wt") as f:
+        json.dump({"source": "WFA2-lib v2.3 built from the reference sources (oracle/Makefile ref)",
+                   "cases": cases}, f)
+
+
+if __name__ == "__main__":
+    make_utest()
+    make_ref_cases()

@@ -1,0 +1,71 @@
+"""The CPU oracle (oracle/biwfa_oracle.c) pinned against WFA2-lib's golden files and
+against the real WFA2-lib built from the reference sources."""
+import numpy as np
+import pytest
+
+from golden_data import printed_line, ref_cases, utest
+from oracle import binding
+
+UTEST_NAMES = sorted(utest()["sets"].keys())
+
+
+@pytest.mark.parametrize("name", UTEST_NAMES)
+def test_oracle_matches_wfa2_utest_goldens(name):
+    data = utest()
+    s = data["sets"][name]
+    pen, score_only = tuple(s["penalties"]), s["score_only"]
+    bad = []
+    for i, (p, t) in enumerate(data["pairs"]):
+        st, score, ops, _ = binding.oracle_align(p, t, pen, score_only)
+        line = printed_line(score, "" if score_only else binding.rle(ops))
+        if st != 0 or line != s["lines"][i]:
+            bad.append(i)
+    assert not bad, f"{name}: {len(bad)} of {len(data['pairs'])} pairs differ, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("case", ref_cases(), ids=lambda c: c["tag"])
+def test_oracle_matches_wfa2_reference_cases(case):
+    pen, score_only = tuple(case["penalties"]), case["score_only"]
+    for p, t, st_ref, score_ref, cig_ref in case["pairs"]:
+        st, score, ops, _ = binding.oracle_align(p, t, pen, score_only)
+        assert st == st_ref
+        assert score == score_ref
+        if not score_only:
+            assert (binding.rle(ops) if ops else "-") == cig_ref
+
+
+def test_oracle_matches_live_reference_on_random_pairs():
+    if binding.build_ref() is None:
+        pytest.skip("WFA2-lib reference sources not mounted here")
+    rng = np.random.default_rng(77)
+    for trial in range(120):
+        n = int(rng.integers(0, 400))
+        p = "".join(rng.choice(list("ACGT"), n))
+        t = list(p)
+        for _ in range(int(rng.integers(0, 40))):
+            if not t:
+                break
+            pos = int(rng.integers(0, len(t)))
+            r = rng.random()
+            if r < 0.4:
+                t[pos] = str(rng.choice(list("ACGT")))
+            elif r < 0.7:
+                t.insert(pos, str(rng.choice(list("ACGT"))) * int(rng.integers(1, 6)))
+            else:
+                del t[pos:pos + int(rng.integers(1, 6))]
+        t = "".join(t)
+        pen = [(0, 4, 6, 2), (0, 1, 2, 1), (0, 5, 3, 2), (-3, 5, 3, 2)][trial % 4]
+        ref = binding.ref_align(p, t, pen)
+        st, score, ops, _ = binding.oracle_align(p, t, pen)
+        assert (st, score, ops) == (ref[0], ref[1], ref[2]), (p, t, pen)
+
+
+def test_oracle_batch_threads_agree_with_single():
+    import biwfa_gpu_pii2025_gb300 as pkg
+    b = pkg.PairBatch.generate(3, 40, seed=9)
+    secs1, s1, st1 = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=1)
+    secs4, s4, st4 = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=4)
+    assert (st1 == 0).all() and (st4 == 0).all()
+    assert (s1 == s4).all()
+    for i in range(0, b.n, 7):
+        assert binding.oracle_align(b.pattern(i), b.text(i))[1] == s1[i]
