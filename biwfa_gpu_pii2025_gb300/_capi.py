@@ -135,8 +135,11 @@ SIGNATURES = {
     "wfg_align_host": (C.c_int, [C.c_void_p, P(Config), C.c_int, C.c_int, C.c_void_p, C.c_int64, _i64p, _ip,
                                  _i64p, _ip, _ip, _ip, _i64p, _ip, _u32p, C.c_int64, _i64p]),
     "wfg_get_stats": (C.c_int, [C.c_void_p, P(Stats)]),
+    "wfg_set_arena_limits": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "wfg_flush_l2": (C.c_int, [C.c_void_p, C.c_int64]),
     "wfg_synchronize": (C.c_int, [C.c_void_p]),
+    "wfg_host_alloc": (C.c_void_p, [C.c_int64]),
+    "wfg_host_free": (None, [C.c_void_p]),
     "wfg_generate": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.c_void_p, _i64p, _i64p, _ip, _i64p, _ip]),
 }
 

@@ -75,6 +75,37 @@ class PairBatch:
         return PairBatch.from_lists([self.pattern(i) for i in idx], [self.text(i) for i in idx])
 
 
+class PinnedHost:
+    """Page-locked host arrays from wfg_host_alloc (freed on close)."""
+
+    def __init__(self):
+        self.lib = _capi.load()
+        self._ptrs = []
+
+    def empty(self, n: int, dtype) -> np.ndarray:
+        dtype = np.dtype(dtype)
+        nbytes = max(int(n) * dtype.itemsize, dtype.itemsize)
+        p = self.lib.wfg_host_alloc(nbytes)
+        if not p:
+            raise MemoryError(f"wfg_host_alloc({nbytes}) failed")
+        self._ptrs.append(p)
+        return np.frombuffer((C.c_uint8 * nbytes).from_address(p), dtype=dtype)[: int(n)]
+
+    def copy(self, a: np.ndarray) -> np.ndarray:
+        out = self.empty(a.size, a.dtype)
+        out[...] = a.reshape(-1)
+        return out
+
+    def batch(self, b: "PairBatch") -> "PairBatch":
+        return PairBatch(self.copy(b.seq), self.copy(b.p_off), self.copy(b.plen), self.copy(b.t_off),
+                         self.copy(b.tlen))
+
+    def close(self):
+        for p in self._ptrs:
+            self.lib.wfg_host_free(p)
+        self._ptrs = []
+
+
 @dataclass
 class BatchResult:
     scores: np.ndarray
@@ -141,6 +172,9 @@ class BatchAligner:
         order = np.ascontiguousarray(order, np.int32)
         self._check(self.lib.wfg_set_order(self.ctx, _ptr(order, _ip)), "wfg_set_order")
 
+    def set_arena_limits(self, ring_w: int = 0, leaf_words: int = 0):
+        self._check(self.lib.wfg_set_arena_limits(self.ctx, ring_w, leaf_words), "wfg_set_arena_limits")
+
     def set_predictions(self, pred: np.ndarray):
         pred = np.ascontiguousarray(pred, np.float32)
         self._check(self.lib.wfg_set_predictions(self.ctx, pred.ctypes.data_as(C.POINTER(C.c_float))),
@@ -163,6 +197,21 @@ class BatchAligner:
                                 _ptr(run_len, _ip), _ptr(runs, _u32p), runs_cap, C.byref(total))
         self._check(st, "wfg_fetch")
         return BatchResult(scores, status, run_off, run_len, runs[:total.value])
+
+    def align_into(self, b: PairBatch, out: BatchResult, penalties=(0, 4, 6, 2), score_only=False,
+                   sched=_capi.SCHED_PLAIN) -> int:
+        """End to end through wfg_align_host into caller-owned (e.g. pinned) output arrays.
+        Returns the number of CIGAR runs written to out.runs."""
+        cfg = self.config(penalties, score_only, 0)
+        total = C.c_int64(0)
+        st = self.lib.wfg_align_host(
+            self.ctx, C.byref(cfg), sched, b.n, b.seq.ctypes.data_as(C.c_void_p), int(b.seq.shape[0]),
+            _ptr(b.p_off, _i64p), _ptr(b.plen, _ip), _ptr(b.t_off, _i64p), _ptr(b.tlen, _ip),
+            _ptr(out.scores, _ip), _ptr(out.status, _ip), _ptr(out.run_off, _i64p), _ptr(out.run_len, _ip),
+            _ptr(out.runs, _u32p), int(out.runs.shape[0]), C.byref(total))
+        self._check(st, "wfg_align_host")
+        self.n = b.n
+        return int(total.value)
 
     def align(self, b: PairBatch, penalties=(0, 4, 6, 2), score_only=False, sched=_capi.SCHED_PLAIN,
               max_steps=0) -> BatchResult:

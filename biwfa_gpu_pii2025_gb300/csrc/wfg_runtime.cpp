@@ -122,6 +122,7 @@ struct wfg_context {
   wfg_stats_t stats{};
   bool ran = false;
   int last_score_only = 0;
+  int limit_ring_w = 0, limit_leaf_words = 0;
 };
 
 static int fail(wfg_context* c, cudaError_t e, const char* where) {
@@ -283,6 +284,7 @@ int leaf_score_bound(const IntPen& p) {
 }
 
 PassShape shape_pass(const wfg_context* c, const IntPen& p, int pass, int ring_w_hint) {
+  if (pass == 0 && c->limit_ring_w > 0) ring_w_hint = c->limit_ring_w;
   PassShape s;
   const int maxsum = std::max(c->max_sum, 1);
   const uint32_t ring_full = next_pow2((uint64_t)maxsum + 8);
@@ -299,6 +301,7 @@ PassShape shape_pass(const wfg_context* c, const IntPen& p, int pass, int ring_w
   if (pass == 0) {
     s.ring_w = ring_w_hint > 0 ? (int)std::min<uint32_t>(next_pow2((uint64_t)ring_w_hint), ring_full) : (int)ring_full;
     s.leaf_words = (int)std::min<int64_t>(leaf_full, 1 << 16);
+    if (c->limit_leaf_words > 0) s.leaf_words = std::max(c->limit_leaf_words, 16);
   } else if (pass == 1) {
     s.ring_w = (int)ring_full;
     s.leaf_words = (int)std::min<int64_t>(leaf_full, 1 << 18);
@@ -350,10 +353,12 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[(size_t)a] > cost[(size_t)b]; });
     ring_hint = (int)(2.0 * (1.25 * maxpred + 64) / std::max(p.e, 1) + 16);
   } else {
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-      return c->h_plen[(size_t)a] + c->h_tlen[(size_t)a] > c->h_plen[(size_t)b] + c->h_tlen[(size_t)b];
-    });
+    // Plain path: longest pairs first, a stable counting sort on plen + tlen (O(n)).
+    std::vector<int> cnt((size_t)c->max_sum + 2, 0);
+    for (int i = 0; i < n; ++i) cnt[(size_t)(c->max_sum - (c->h_plen[(size_t)i] + c->h_tlen[(size_t)i])) + 1]++;
+    for (size_t v = 1; v < cnt.size(); ++v) cnt[v] += cnt[v - 1];
+    for (int i = 0; i < n; ++i)
+      order[(size_t)cnt[(size_t)(c->max_sum - (c->h_plen[(size_t)i] + c->h_tlen[(size_t)i]))]++] = i;
   }
   // ---- pass shapes and arena
   int bps = 0;
@@ -491,6 +496,23 @@ int wfg_align_host(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched,
   st = wfg_run(c, cfg, sched);
   if (st != WF_STATUS_ALG_COMPLETED) return st;
   return wfg_fetch(c, scores, statuses, run_off, run_len, runs, runs_cap, total_runs);
+}
+
+void* wfg_host_alloc(int64_t bytes) {
+  void* p = nullptr;
+  if (bytes <= 0 || cudaMallocHost(&p, (size_t)bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void wfg_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+int wfg_set_arena_limits(wfg_context_t* c, int ring_w, int leaf_words) {
+  if (!c || ring_w < 0 || leaf_words < 0) return WF_STATUS_UNSUPPORTED;
+  c->limit_ring_w = ring_w;
+  c->limit_leaf_words = leaf_words;
+  return WF_STATUS_ALG_COMPLETED;
 }
 
 int wfg_flush_l2(wfg_context_t* c, int64_t bytes) {

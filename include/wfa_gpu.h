@@ -266,10 +266,18 @@ int wfg_align_host(wfg_context_t* ctx, const wfg_config_t* cfg, wfg_sched_t sche
                    int* scores, int* statuses, int64_t* run_off, int* run_len,
                    uint32_t* runs, int64_t runs_cap, int64_t* total_runs);
 int wfg_get_stats(wfg_context_t* ctx, wfg_stats_t* stats);
+/* Caps on the first pass's per-warp arena (0 = automatic): ring width in diagonals and
+ * leaf store in int32 words. Pairs that do not fit overflow into the retry passes, whose
+ * arenas are sized from the batch's longest pair; results never change. */
+int wfg_set_arena_limits(wfg_context_t* ctx, int ring_w, int leaf_words);
 /* Write ~bytes of scratch to evict the L2 (between timed runs). */
 int wfg_flush_l2(wfg_context_t* ctx, int64_t bytes);
 /* Synchronize the context's stream. */
 int wfg_synchronize(wfg_context_t* ctx);
+/* Page-locked host memory for inputs/outputs (copies to and from it run at full link
+ * speed). NULL on failure. */
+void* wfg_host_alloc(int64_t bytes);
+void wfg_host_free(void* ptr);
 
 /* Seeded synthetic pair generator (host; deterministic on every platform).
  * workload: 1 = 1 kbp / 5 % (sub/ins/del 1/3 each, single-base indels),

@@ -112,8 +112,8 @@ def ref_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False):
 
 
 def oracle_batch_time(seq: np.ndarray, p_off, plen, t_off, tlen, penalties=(0, 4, 6, 2), score_only=False,
-                      threads: int = 1):
-    """Aligns a batch with the oracle on `threads` POSIX threads; returns (seconds, scores, status)."""
+                      threads: int = 1, return_ops: bool = False):
+    """Aligns a batch with the oracle on `threads` POSIX threads; returns (seconds, scores, status[, ops])."""
     lib = oracle_lib()
     n = int(len(plen))
     p_off = np.ascontiguousarray(p_off, np.int64); t_off = np.ascontiguousarray(t_off, np.int64)
@@ -130,4 +130,7 @@ def oracle_batch_time(seq: np.ndarray, p_off, plen, t_off, tlen, penalties=(0, 4
         C.c_int(penalties[0]), C.c_int(penalties[1]), C.c_int(penalties[2]), C.c_int(penalties[3]),
         C.c_int(1 if score_only else 0), ops.ctypes.data_as(C.c_char_p), ops_off.ctypes.data_as(i64p),
         scores.ctypes.data_as(ip), status.ctypes.data_as(ip), ops_len.ctypes.data_as(ip), C.c_int(threads))
+    if return_ops:
+        cig = [ops[ops_off[i]:ops_off[i] + ops_len[i]].tobytes().decode() for i in range(n)]
+        return float(secs), scores, status, cig
     return float(secs), scores, status

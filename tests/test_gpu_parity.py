@@ -1,0 +1,178 @@
+"""GPU parity: the CUDA path, called through the C ABI, against WFA2-lib's goldens, the real
+WFA2-lib's recorded outputs, and the oracle — bit-exact scores and CIGARs."""
+import numpy as np
+import pytest
+
+import biwfa_gpu_pii2025_gb300 as pkg
+from biwfa_gpu_pii2025_gb300 import _capi
+from golden_data import printed_line, ref_cases, utest
+from oracle import binding
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_printed_line(res, i, score_only):
+    """The GPU result in align_benchmark's `score\\tCIGAR` form."""
+    if score_only:
+        return printed_line(int(res.scores[i]), "")
+    cig = res.cigar(i)
+    return printed_line(int(res.scores[i]) if cig else -1, cig)
+
+
+@pytest.mark.parametrize("name", sorted(utest()["sets"].keys()))
+def test_gpu_matches_wfa2_utest_goldens(batch_aligner, name):
+    data = utest()
+    s = data["sets"][name]
+    b = pkg.PairBatch.from_lists([p for p, _ in data["pairs"]], [t for _, t in data["pairs"]])
+    res = batch_aligner.align(b, penalties=tuple(s["penalties"]), score_only=s["score_only"])
+    assert (res.status == 0).all()
+    bad = [i for i in range(b.n) if gpu_printed_line(res, i, s["score_only"]) != s["lines"][i]]
+    assert not bad, f"{name}: {len(bad)} pairs differ, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("case", ref_cases(), ids=lambda c: c["tag"])
+def test_gpu_matches_wfa2_reference_outputs(batch_aligner, case):
+    pairs = case["pairs"]
+    b = pkg.PairBatch.from_lists([r[0] for r in pairs], [r[1] for r in pairs])
+    res = batch_aligner.align(b, penalties=tuple(case["penalties"]), score_only=case["score_only"])
+    for i, (_, _, st, score, cig) in enumerate(pairs):
+        assert res.status[i] == st, i
+        assert gpu_printed_line(res, i, case["score_only"]) == printed_line(score, "" if case["score_only"] else
+                                                                           (cig if cig != "-" else "")), i
+
+
+@pytest.mark.parametrize("workload,n,seed", [(1, 300, 11), (2, 2000, 12), (3, 60, 13), (5, 400, 15)])
+def test_gpu_matches_oracle_on_generated(batch_aligner, workload, n, seed):
+    b = pkg.PairBatch.generate(workload, n, seed)
+    res = batch_aligner.align(b)
+    _, scores, status, ops = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=8,
+                                                       return_ops=True)
+    assert (status == 0).all() and (res.status == 0).all()
+    bad = [i for i in range(b.n) if pkg.runs_to_ops(res.runs_of(i)) != ops[i] or
+           res.scores[i] != (scores[i] if ops[i] else 0)]
+    assert not bad, f"{len(bad)} pairs differ, first {bad[:5]}"
+
+
+def test_gpu_long_noisy_pair_matches_oracle(batch_aligner):
+    b = pkg.PairBatch.generate(4, 2, seed=404)
+    res = batch_aligner.align(b)
+    for i in range(b.n):
+        st, score, ops, _ = binding.oracle_align(b.pattern(i), b.text(i))
+        assert res.status[i] == 0
+        assert res.scores[i] == score
+        assert pkg.runs_to_ops(res.runs_of(i)) == ops
+
+
+def test_gpu_score_only_matches_oracle(batch_aligner):
+    b = pkg.PairBatch.generate(5, 300, seed=21)
+    res = batch_aligner.align(b, score_only=True)
+    assert (res.status == 0).all()
+    assert (res.run_len == 0).all()
+    for i in range(b.n):
+        assert res.scores[i] == binding.oracle_align(b.pattern(i), b.text(i), score_only=True)[1]
+
+
+def test_overflow_retry_passes_keep_results_exact(batch_aligner):
+    """Tiny first-pass arenas push most pairs into the retry passes; results must not move."""
+    b = pkg.PairBatch.generate(5, 200, seed=31)
+    ref = batch_aligner.align(b)
+    try:
+        batch_aligner.set_arena_limits(ring_w=16, leaf_words=64)
+        res = batch_aligner.align(b)
+        st = batch_aligner.stats()
+    finally:
+        batch_aligner.set_arena_limits(0, 0)
+    assert st.retried_pairs > 0
+    assert (res.status == 0).all()
+    assert np.array_equal(res.scores, ref.scores)
+    for i in range(b.n):
+        assert np.array_equal(res.runs_of(i), ref.runs_of(i))
+
+
+def test_given_order_and_predictions_do_not_change_results(batch_aligner):
+    b = pkg.PairBatch.generate(5, 300, seed=41)
+    ref = batch_aligner.align(b)
+    batch_aligner.upload(b)
+    batch_aligner.set_order(np.random.default_rng(0).permutation(b.n))
+    batch_aligner.run(sched=_capi.SCHED_GIVEN)
+    r2 = batch_aligner.fetch()
+    batch_aligner.upload(b)
+    batch_aligner.set_predictions(np.random.default_rng(1).uniform(0, 3000, b.n))
+    batch_aligner.run(sched=_capi.SCHED_LEARNED)
+    r3 = batch_aligner.fetch()
+    for r in (r2, r3):
+        assert np.array_equal(r.scores, ref.scores) and np.array_equal(r.status, ref.status)
+        for i in range(b.n):
+            assert np.array_equal(r.runs_of(i), ref.runs_of(i))
+
+
+def test_wfa2_single_pair_api():
+    data = utest()
+    s = data["sets"]["test.biwfa.affine.alg"]
+    al = pkg.WavefrontAligner(0, 4, 6, 2)
+    try:
+        for i in (0, 5, 77, 150, 304):
+            p, t = data["pairs"][i]
+            assert al.align(p, t) == _capi.WF_STATUS_ALG_COMPLETED
+            assert al.status == 0
+            line = printed_line(al.cigar_score(), al.cigar_str())
+            assert line == s["lines"][i]
+            assert al.score == al.cigar_score()
+            sam = al.sam_cigar(True)
+            assert sum(x >> 4 for x in sam) == len(al.cigar_ops())
+        # empty inputs
+        assert al.align("", "") == 0 and al.cigar_str() == ""
+        assert al.align("ACGT", "") == 0 and al.cigar_str() == "4D" and al.score == -(6 + 2 * 4)
+        st, out = al.align_batch(["GATTACA", "ACGT"], ["GATCACA", "ACGT"])
+        assert st == 0 and out[0] == (0, -4, "3M1X3M") and out[1] == (0, 0, "4M")
+    finally:
+        al.close()
+
+
+def test_wfa2_api_refuses_unsupported_configurations():
+    for kw in (dict(memory_mode=_capi.WAVEFRONT_MEMORY_HIGH), dict(heuristic=_capi.WF_HEURISTIC_WFADAPTIVE),
+               dict(match=1), dict(mismatch=0)):
+        al = pkg.WavefrontAligner(**kw)
+        try:
+            assert al.align("ACGT", "ACGT") == _capi.WF_STATUS_UNSUPPORTED
+        finally:
+            al.close()
+
+
+def _check_properties(b, res, penalties=(0, 4, 6, 2)):
+    """Size-independent checks of every pair: status, consumed lengths, score = rescore(CIGAR)."""
+    m, x, o, e = penalties
+    assert (res.status == 0).all()
+    runs = res.runs.astype(np.int64)
+    op = runs & 15
+    ln = runs >> 4
+    pair_of = np.repeat(np.arange(b.n), res.run_len)
+    order = np.argsort(res.run_off, kind="stable")
+    # runs are contiguous per pair: rebuild pair ids in run-buffer order
+    pair_of = np.empty(runs.shape[0], np.int64)
+    for_pos = np.repeat(order, res.run_len[order])
+    pair_of[:] = for_pos
+    cons_p = np.bincount(pair_of, weights=ln * np.isin(op, [7, 8, 2]), minlength=b.n)
+    cons_t = np.bincount(pair_of, weights=ln * np.isin(op, [7, 8, 1]), minlength=b.n)
+    assert np.array_equal(cons_p.astype(np.int64), b.plen.astype(np.int64))
+    assert np.array_equal(cons_t.astype(np.int64), b.tlen.astype(np.int64))
+    pen = np.where(op == 7, -m * ln, np.where(op == 8, -x * ln, -(o + e * ln)))
+    sc = np.bincount(pair_of, weights=pen, minlength=b.n).astype(np.int64)
+    assert np.array_equal(sc, res.scores.astype(np.int64))
+    # adjacent runs of one pair never share an op (maximal runs)
+    same = (pair_of[1:] == pair_of[:-1]) & (op[1:] == op[:-1])
+    assert not same.any()
+
+
+@pytest.mark.parametrize("workload,n,sample", [(1, 10_000, 10_000), (2, 1_000_000, 20_000), (3, 200_000, 2_000)])
+def test_full_size_workloads(batch_aligner, workload, n, sample):
+    """Full-size workloads: every pair checked by properties; a seeded sample bit-exact vs the oracle."""
+    b = pkg.PairBatch.generate(workload, n, seed=5000 + workload)
+    res = batch_aligner.align(b)
+    _check_properties(b, res)
+    idx = np.sort(np.random.default_rng(workload).choice(n, size=sample, replace=False))
+    sub = b.subset(idx)
+    _, scores, status, ops = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen,
+                                                       threads=16, return_ops=True)
+    bad = [j for j, i in enumerate(idx) if pkg.runs_to_ops(res.runs_of(i)) != ops[j] or res.scores[i] != scores[j]]
+    assert not bad, f"{len(bad)} of {sample} sampled pairs differ"
