@@ -680,7 +680,7 @@ __global__ void __launch_bounds__(WPB * 32) biwfa_persistent_kernel(KernelParams
     if (lane == 0) {
       P.scores[pi] = score;
       P.status[pi] = status;
-      if (status != WFG_ST_COMPLETED) { P.run_off[pi] = 0; P.run_len[pi] = 0; }
+      if (status != WFG_ST_COMPLETED || P.score_only) { P.run_off[pi] = 0; P.run_len[pi] = 0; }
       if (P.stats) {
         P.stats[pi * 4 + 0] = nsteps;
         P.stats[pi * 4 + 1] = max_leaf;

@@ -332,7 +332,9 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   }
   cudaSetDevice(c->device);
   const int n = c->n;
+  const int64_t h2d_upload = c->stats.h2d_bytes;
   c->stats = wfg_stats_t{};
+  c->stats.h2d_bytes = h2d_upload + (int64_t)sizeof(int) * n;  // upload + processing order
   c->last_score_only = cfg->score_only;
   // ---- order
   std::vector<int> order((size_t)n);

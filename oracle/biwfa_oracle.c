@@ -60,6 +60,25 @@ static void wf_reserve(wf_t* w, int lo, int hi) {
   w->cap = len + 2 * pad;
   w->off = (int32_t*)malloc(sizeof(int32_t) * (size_t)w->cap);
 }
+/* Make k in [need_lo, need_hi] readable without range checks: values outside the
+ * wavefront's [lo, hi] read as OFF_NULL (the init_ends of
+ * wavefront/wavefront_compute.c:498-575). Returns a k-indexed pointer. */
+static const int32_t* wf_padded(wf_t* w, int need_lo, int need_hi) {
+  if (need_lo < w->base || need_hi >= w->base + w->cap) {
+    const int lo = need_lo < w->lo ? need_lo : w->lo, hi = need_hi > w->hi ? need_hi : w->hi;
+    const int len = hi - lo + 1, pad = len / 2 + 16;
+    int32_t* nb = (int32_t*)malloc(sizeof(int32_t) * (size_t)(len + 2 * pad));
+    const int nbase = lo - pad;
+    if (w->lo <= w->hi)
+      memcpy(nb + (w->lo - nbase), w->off + (w->lo - w->base), sizeof(int32_t) * (size_t)(w->hi - w->lo + 1));
+    free(w->off);
+    w->off = nb; w->base = nbase; w->cap = len + 2 * pad;
+  }
+  int32_t* p = w->off - w->base;
+  for (int k = need_lo; k < w->lo && k <= need_hi; ++k) p[k] = OFF_NULL;
+  for (int k = (w->hi + 1 > need_lo ? w->hi + 1 : need_lo); k <= need_hi; ++k) p[k] = OFF_NULL;
+  return p;
+}
 
 typedef struct {
   int x, o, e;        /* internal (possibly transformed) penalties */
@@ -85,6 +104,8 @@ typedef struct {
   int num_null_steps;
   int status, status_score;
   int end_k, end_off;
+  wf_t nullw;               /* all-NULL storage standing in for absent inputs */
+  wf_t victim;              /* write-only sink for outputs that are not kept */
 } dir_t;
 
 static void dir_alloc(dir_t* d, const pen_t* pen, counters_t* cnt, int modular, int nslots) {
@@ -106,6 +127,8 @@ static void dir_grow(dir_t* d, int nslots) {
 }
 static void dir_free(dir_t* d) {
   for (int i = 0; i < d->nslots; ++i) { free(d->M[i].off); free(d->I[i].off); free(d->D[i].off); }
+  free(d->nullw.off);
+  free(d->victim.off);
   free(d->M); free(d->I); free(d->D);
 }
 static inline int dir_slot(const dir_t* d, int score) {
@@ -128,13 +151,28 @@ static void dir_init(dir_t* d, const char* pat, int plen, const char* txt, int t
 
 /* Fetch an input wavefront: NULL when score < 0, the slot is empty or the wavefront
  * is null (wavefront_compute_get_*wavefront, wavefront/wavefront_compute.c:249-285). */
-static inline const wf_t* fetch(const dir_t* d, const wf_t* comp, int score) {
+static inline wf_t* fetch(const dir_t* d, wf_t* comp, int score) {
   if (score < 0) return NULL;
   int s = score;
   if (d->modular && s > 0) s = s % d->pen->scope;
   if (!d->modular && s >= d->nslots) return NULL;
-  const wf_t* w = &comp[s];
+  wf_t* w = &comp[s];
   return wf_null(w) ? NULL : w;
+}
+
+/* k-indexed all-NULL array covering [need_lo, need_hi] (the shared null wavefront). */
+static const int32_t* null_padded(dir_t* d, int need_lo, int need_hi) {
+  wf_t* w = &d->nullw;
+  if (w->off == NULL || need_lo < w->base || need_hi >= w->base + w->cap) {
+    const int lo = (w->off && w->base < need_lo) ? w->base : need_lo;
+    const int hi = (w->off && w->base + w->cap - 1 > need_hi) ? w->base + w->cap - 1 : need_hi;
+    const int len = hi - lo + 1, pad = len / 2 + 64;
+    free(w->off);
+    w->base = lo - pad; w->cap = len + 2 * pad;
+    w->off = (int32_t*)malloc(sizeof(int32_t) * (size_t)w->cap);
+    for (int i = 0; i < w->cap; ++i) w->off[i] = OFF_NULL;
+  }
+  return w->off - w->base;
 }
 
 /* Trim out-of-bounds ends (wavefront_compute_trim_ends, wavefront/wavefront_compute.c:579-613). */
@@ -160,10 +198,10 @@ static void trim_ends(const dir_t* d, wf_t* w) {
 static void dir_compute(dir_t* d, int score) {
   const pen_t* p = d->pen;
   if (!d->modular && score >= d->nslots) dir_grow(d, score + 1 > 2 * d->nslots ? score + 1 : 2 * d->nslots);
-  const wf_t* mx = fetch(d, d->M, score - p->x);
-  const wf_t* mo = fetch(d, d->M, score - p->o - p->e);
-  const wf_t* ie = fetch(d, d->I, score - p->e);
-  const wf_t* de = fetch(d, d->D, score - p->e);
+  wf_t* mx = fetch(d, d->M, score - p->x);
+  wf_t* mo = fetch(d, d->M, score - p->o - p->e);
+  wf_t* ie = fetch(d, d->I, score - p->e);
+  wf_t* de = fetch(d, d->D, score - p->e);
   const int slot = dir_slot(d, score);
   wf_t* om = &d->M[slot]; wf_t* oi = &d->I[slot]; wf_t* od = &d->D[slot];
   d->cnt->n_steps++;
@@ -188,18 +226,34 @@ static void dir_compute(dir_t* d, int score) {
   if (alloc_d) { wf_reserve(od, lo, hi); od->present = 1; od->lo = lo; od->hi = hi; } else od->present = 0;
   d->cnt->n_cells += 3 * (int64_t)(hi - lo + 1);
   const uint32_t tl = (uint32_t)d->tlen, pl = (uint32_t)d->plen;
+  /* NULL-padded k-indexed inputs (mx and mo may be the same wavefront when x == o + e). */
+  const int32_t *pmx, *pmo;
+  if (mx != NULL && mx == mo) {
+    pmx = pmo = wf_padded(mx, lo - 1, hi + 1);
+  } else {
+    pmo = mo ? wf_padded(mo, lo - 1, hi + 1) : null_padded(d, lo - 1, hi + 1);
+    pmx = mx ? wf_padded(mx, lo, hi) : null_padded(d, lo - 1, hi + 1);
+  }
+  const int32_t* pie = ie ? wf_padded(ie, lo - 1, hi - 1) : null_padded(d, lo - 1, hi + 1);
+  const int32_t* pde = de ? wf_padded(de, lo + 1, hi + 1) : null_padded(d, lo - 1, hi + 1);
+  /* Outputs that WFA2 sends to its victim wavefront go to a scratch array here, so the
+   * loop below has no branches (wavefront_compute.c:382-494). */
+  wf_reserve(&d->victim, lo, hi);
+  int32_t* qm = om->off - om->base;
+  int32_t* qi = alloc_i ? oi->off - oi->base : d->victim.off - d->victim.base;
+  int32_t* qd = alloc_d ? od->off - od->base : d->victim.off - d->victim.base;
   for (int k = lo; k <= hi; ++k) {
-    const int32_t ins_o = wf_get(mo, k - 1), ins_e = wf_get(ie, k - 1);
+    const int32_t ins_o = pmo[k - 1], ins_e = pie[k - 1];
     const int32_t ins = (ins_o >= ins_e ? ins_o : ins_e) + 1;
-    const int32_t del_o = wf_get(mo, k + 1), del_e = wf_get(de, k + 1);
+    const int32_t del_o = pmo[k + 1], del_e = pde[k + 1];
     const int32_t del = (del_o >= del_e ? del_o : del_e);
-    const int32_t mis = wf_get(mx, k) + 1;
+    const int32_t mis = pmx[k] + 1;
     int32_t m = mis >= ins ? mis : ins;
     m = del >= m ? del : m;
     if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = OFF_NULL;
-    if (alloc_i) oi->off[k - oi->base] = ins;
-    if (alloc_d) od->off[k - od->base] = del;
-    om->off[k - om->base] = m;
+    qi[k] = ins;
+    qd[k] = del;
+    qm[k] = m;
   }
   trim_ends(d, om);
   if (alloc_i) trim_ends(d, oi);
@@ -210,15 +264,18 @@ static void dir_compute(dir_t* d, int score) {
  * wavefront_extend_matches_kernel_blockwise (wavefront_extend_kernels.c:68-92)
  * written with explicit window bounds instead of EOS characters. */
 static inline int lcp(const char* P, int plen, const char* T, int tlen, int v, int h) {
+  const int maxn = (plen - v < tlen - h) ? plen - v : tlen - h;
+  const char* p = P + v;
+  const char* t = T + h;
   int n = 0;
-  while (v + n + 8 <= plen && h + n + 8 <= tlen) {
+  while (n + 8 <= maxn) {
     uint64_t a, b;
-    memcpy(&a, P + v + n, 8); memcpy(&b, T + h + n, 8);
+    memcpy(&a, p + n, 8); memcpy(&b, t + n, 8);
     const uint64_t x = a ^ b;
     if (x) return n + (__builtin_ctzll(x) >> 3);
     n += 8;
   }
-  while (v + n < plen && h + n < tlen && P[v + n] == T[h + n]) ++n;
+  while (n < maxn && p[n] == t[n]) ++n;
   return n;
 }
 
@@ -246,16 +303,22 @@ static int dir_extend(dir_t* d, int score, int* max_ak_out) {
     return 0;
   }
   int max_ak = 0;
-  for (int k = m->lo; k <= m->hi; ++k) {
-    int32_t off = m->off[k - m->base];
+  int32_t* const offs = m->off - m->base;
+  const char* const P = d->pat;
+  const char* const T = d->txt;
+  const int plen = d->plen, tlen = d->tlen, lo = m->lo, hi = m->hi;
+  int64_t ext = 0;
+  for (int k = lo; k <= hi; ++k) {
+    int32_t off = offs[k];
     if (off == OFF_NULL) continue;
-    const int n = lcp(d->pat, d->plen, d->txt, d->tlen, off - k, off);
-    d->cnt->n_ext += n + 1;
+    const int n = lcp(P, plen, T, tlen, off - k, off);
+    ext += n + 1;
     off += n;
-    m->off[k - m->base] = off;
+    offs[k] = off;
     const int ak = 2 * off - k;
     if (max_ak < ak) max_ak = ak;
   }
+  d->cnt->n_ext += ext;
   if (termination(d, score)) {
     d->status = ST_END_REACHED; d->status_score = score; return 1;
   }
