@@ -140,6 +140,9 @@ SIGNATURES = {
     "wfg_synchronize": (C.c_int, [C.c_void_p]),
     "wfg_host_alloc": (C.c_void_p, [C.c_int64]),
     "wfg_host_free": (None, [C.c_void_p]),
+    "wfg_align_noalloc": (C.c_int, [P(Config), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                    C.c_void_p]),
     "wfg_generate": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.c_void_p, _i64p, _i64p, _ip, _i64p, _ip]),
 }
 

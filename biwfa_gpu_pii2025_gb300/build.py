@@ -22,7 +22,7 @@ LIB = PKG / "libbiwfa_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
-SOURCES = ["biwfa_kernel.cu", "wfg_runtime.cpp", "wfa2_compat.cpp", "datagen.cpp"]
+SOURCES = ["biwfa_kernel.cu", "wfg_runtime.cpp", "wfa2_compat.cpp", "datagen.cpp", "noalloc.cu"]
 
 
 def nvcc_path() -> str:

@@ -91,11 +91,11 @@ struct ArenaLayout {
   int64_t total;
 };
 
-WFG_HD static inline int64_t wfg_align256(int64_t v) { return (v + 255) & ~(int64_t)255; }
+WFG_HD constexpr inline int64_t wfg_align256(int64_t v) { return (v + 255) & ~(int64_t)255; }
 
-WFG_HD static inline ArenaLayout wfg_arena_layout(int scope, int ring_w, int leaf_max_score, int leaf_words,
+WFG_HD constexpr inline ArenaLayout wfg_arena_layout(int scope, int ring_w, int leaf_max_score, int leaf_words,
                                            int run_cap, int leaf_run_cap, int stack_cap) {
-  ArenaLayout L;
+  ArenaLayout L{};
   int64_t off = 0;
   L.ring_off = off; L.ring_bytes = wfg_align256((int64_t)2 * scope * 3 * ring_w * 4); off += L.ring_bytes;
   L.ldesc_off = off; L.ldesc_bytes = wfg_align256((int64_t)(leaf_max_score + 1) * 3 * 16); off += L.ldesc_bytes;

@@ -279,6 +279,32 @@ int wfg_synchronize(wfg_context_t* ctx);
 void* wfg_host_alloc(int64_t bytes);
 void wfg_host_free(void* ptr);
 
+/* Aligning without allocating (no WFA2-lib counterpart; there is no reference interface
+ * this replaces). For callers that may not allocate device memory themselves or let a
+ * library do it — code inside a framework that owns every device allocation, or code
+ * that must not allocate while latency-critical work runs. The caller passes device
+ * pointers to its inputs (sequence bytes, per-pair offsets and lengths) and to its
+ * outputs (scores, statuses, run offsets and lengths, and a runs buffer of runs_cap
+ * entries) and a cudaStream_t (or NULL); everything else lives in a fixed 28 MiB
+ * __device__ array inside the library, held by every GPU that loads it until exit.
+ * No cudaMalloc, cudaFree or other allocating call is made.
+ *   - The first call on a device looks up that array's address (with that device
+ *     current); make that first call before any stream capture.
+ *   - Calls share the array: calls that overlap on the GPU race. Serialize them.
+ *   - Limits per call: at most WFG_NOALLOC_MAX_PAIRS pairs (else WF_STATUS_UNSUPPORTED
+ *     is returned and nothing runs); pairs with plen + tlen above
+ *     WFG_NOALLOC_MAX_PAIR_LEN get status WF_STATUS_UNSUPPORTED; penalties whose score
+ *     scope max(o+e, x)+1 exceeds 16 are refused; a pair that outgrows the fixed arena
+ *     gets WF_STATUS_OOM.
+ * Returns WF_STATUS_ALG_COMPLETED once the work is enqueued on the stream; per-pair
+ * results (same as wfg_run's) are valid after the stream completes. */
+#define WFG_NOALLOC_MAX_PAIRS 4096
+#define WFG_NOALLOC_MAX_PAIR_LEN 1024
+int wfg_align_noalloc(const wfg_config_t* cfg, int num_pairs, const char* d_seq,
+                      const int64_t* d_p_off, const int* d_plen, const int64_t* d_t_off, const int* d_tlen,
+                      int* d_scores, int* d_status, int64_t* d_run_off, int* d_run_len,
+                      uint32_t* d_runs, int64_t runs_cap, void* stream);
+
 /* Seeded synthetic pair generator (host; deterministic on every platform).
  * workload: 1 = 1 kbp / 5 % (sub/ins/del 1/3 each, single-base indels),
  *           2 = 150 bp / 2 %, 3 = uneven: log-uniform 100..10000 bp, 1..10 % error,
