@@ -27,6 +27,7 @@ constexpr int32_t kNull = INT32_MIN / 2;   // WAVEFRONT_OFFSET_NULL
 constexpr int kAbsent = INT32_MAX;         // lo of a wavefront that does not exist
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxScope = 32;
+constexpr int kMinBlocksPerSM = 6;  // caps registers so 24 warps fit on an SM
 constexpr int ST_OK = -1, ST_END_REACHED = -2, ST_END_UNREACHABLE = -3;
 constexpr int CM = 0, CI = 1, CD = 3;      // components (affine2p_matrix_type values)
 constexpr int kFallbackMinScore = 250, kFallbackMinLength = 100, kRecoveryMinScore = 500;
@@ -58,20 +59,21 @@ __device__ __forceinline__ WfRef absent_ref() {
 struct Pen { int x, o, e, scope; };
 
 // Oriented window over packed words (forward arrays for the forward aligner and the
-// leaf, reversed arrays for the reverse aligner).
+// leaf, reversed arrays for the reverse aligner). bshift = log2(bits per character).
 struct SeqView {
   const uint32_t* pw;
   const uint32_t* tw;
   int p0, t0;
   int plen, tlen;
-  int bits;
+  int bshift;
 };
 
 // 32-bit window of packed characters starting at character pos (first char in the low bits).
-__device__ __forceinline__ uint32_t win32(const uint32_t* w, int pos, int bits) {
-  const uint32_t bit = (uint32_t)pos * (uint32_t)bits;
+// The packed words are read-only while the alignment kernel runs.
+__device__ __forceinline__ uint32_t win32(const uint32_t* w, int pos, int bshift) {
+  const uint32_t bit = (uint32_t)pos << bshift;
   const uint32_t wi = bit >> 5;
-  return __funnelshift_r(w[wi], w[wi + 1], bit & 31u);
+  return __funnelshift_r(__ldg(w + wi), __ldg(w + wi + 1), bit & 31u);
 }
 
 // Longest common extension of P[v..] and T[h..] inside the window: the sentinel-bounded
@@ -79,93 +81,107 @@ __device__ __forceinline__ uint32_t win32(const uint32_t* w, int pos, int bits) 
 __device__ __forceinline__ int lcp(const SeqView& s, int v, int h) {
   const int maxn = min(s.plen - v, s.tlen - h);
   if (maxn <= 0) return 0;
-  const int cpw = 32 / s.bits;
+  const int cpw = 32 >> s.bshift;
   int n = 0;
   for (;;) {
-    const uint32_t x = win32(s.pw, s.p0 + v + n, s.bits) ^ win32(s.tw, s.t0 + h + n, s.bits);
-    if (x) { n += (__ffs((int)x) - 1) / s.bits; break; }
+    const uint32_t x = win32(s.pw, s.p0 + v + n, s.bshift) ^ win32(s.tw, s.t0 + h + n, s.bshift);
+    if (x) { n += (__ffs((int)x) - 1) >> s.bshift; break; }
     n += cpw;
     if (n >= maxn) break;
   }
   return min(n, maxn);
 }
 
+// Storage configuration of one direction, fixed for the kernel's lifetime; functions copy
+// it into registers once per call.
+struct DirCfg {
+  int leaf;          // 0: modular ring (breakpoint search), 1: full store (leaf)
+  int scope;
+  uint32_t magic;    // floor(2^32 / scope) + 1: slot = s - scope * umulhi(s, magic), s < 2^27
+  int W;             // ring width (power of two)
+  int lmax;          // leaf descriptor capacity (scores)
+  int2* rdesc;       // ring descriptors [scope*3] (shared memory)
+  int32_t* rdata;    // ring storage [scope*3][W]
+  int4* ldesc;       // leaf descriptors [(lmax+1)*3] {lo, hi, data_off, kbase}
+  int32_t* ldata;
+};
+
 // One direction of WFA over one window (a wavefront_aligner_t in WFA2). Lives in shared
 // memory; every lane updates its fields with identical values.
 struct Dir {
-  int leaf;          // 0: modular ring (breakpoint search), 1: full store (leaf)
-  int scope;
-  int2* rdesc;       // ring descriptors [scope*3] (shared memory)
-  int32_t* rdata;    // ring storage [scope*3][W]
-  int W;
-  int4* ldesc;       // leaf descriptors [(lmax+1)*3] {lo, hi, data_off, kbase}
-  int32_t* ldata;
-  int lcap, lused, lmax;
+  DirCfg cfg;
+  int lcap, lused;
   SeqView sv;
   int cb, ce;
   int num_null, status, status_score, end_k;
 };
 
-__device__ __forceinline__ WfRef ref_raw(const Dir& d, int score, int ci) {
+__device__ __forceinline__ int slot_of(const DirCfg& c, int score) {
+  return score - c.scope * (int)__umulhi((uint32_t)score, c.magic);
+}
+
+__device__ __forceinline__ WfRef ref_raw(const DirCfg& c, int score, int ci) {
   if (score < 0) return absent_ref();
   WfRef r;
-  if (!d.leaf) {
-    const int slot = score % d.scope;
-    const int2 ds = d.rdesc[slot * 3 + ci];
+  if (!c.leaf) {
+    const int slot = slot_of(c, score);
+    const int2 ds = c.rdesc[slot * 3 + ci];
     r.lo = ds.x; r.hi = ds.y;
-    r.base = d.rdata + (size_t)(slot * 3 + ci) * (size_t)d.W;
-    r.kbase = 0; r.mask = (uint32_t)d.W - 1u;
+    r.base = c.rdata + (size_t)(slot * 3 + ci) * (size_t)c.W;
+    r.kbase = 0; r.mask = (uint32_t)c.W - 1u;
   } else {
-    if (score > d.lmax) return absent_ref();
-    const int4 ds = d.ldesc[score * 3 + ci];
+    if (score > c.lmax) return absent_ref();
+    const int4 ds = c.ldesc[score * 3 + ci];
     r.lo = ds.x; r.hi = ds.y;
-    r.base = d.ldata + ds.z;
+    r.base = c.ldata + ds.z;
     r.kbase = ds.w; r.mask = 0xffffffffu;
   }
   return r;
 }
 // Input fetch: absent when the score is negative, the slot is empty or the wavefront is
 // null (wavefront_compute_get_*wavefront).
-__device__ __forceinline__ WfRef fetch(const Dir& d, int score, int ci) {
-  const WfRef r = ref_raw(d, score, ci);
+__device__ __forceinline__ WfRef fetch(const DirCfg& c, int score, int ci) {
+  const WfRef r = ref_raw(c, score, ci);
   return r.nonnull() ? r : absent_ref();
 }
-__device__ __forceinline__ void set_desc(Dir& d, int score, int ci, int lo, int hi, int data_off, int kbase) {
-  if (!d.leaf) d.rdesc[(score % d.scope) * 3 + ci] = make_int2(lo, hi);
-  else d.ldesc[score * 3 + ci] = make_int4(lo, hi, data_off, kbase);
+__device__ __forceinline__ void set_desc(const DirCfg& c, int score, int ci, int lo, int hi, int data_off, int kbase) {
+  if (!c.leaf) c.rdesc[slot_of(c, score) * 3 + ci] = make_int2(lo, hi);
+  else c.ldesc[score * 3 + ci] = make_int4(lo, hi, data_off, kbase);
 }
 
 // wavefront_aligner_init / init_wf (wavefront/wavefront_aligner.c:251-417)
 __device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
+  const DirCfg c = d.cfg;
   d.sv = sv; d.cb = cb; d.ce = ce;
   d.num_null = 0; d.status = ST_OK; d.status_score = 0; d.end_k = INT_MAX;
   const int cbi = comp_index(cb);
-  if (!d.leaf) {
-    for (int i = 0; i < d.scope * 3; ++i) d.rdesc[i] = make_int2(kAbsent, INT_MIN);
-    d.rdesc[cbi] = make_int2(0, 0);
-    d.rdata[(size_t)cbi * d.W] = 0;  // diagonal 0 of slot 0
+  if (!c.leaf) {
+    for (int i = 0; i < c.scope * 3; ++i) c.rdesc[i] = make_int2(kAbsent, INT_MIN);
+    c.rdesc[cbi] = make_int2(0, 0);
+    c.rdata[(size_t)cbi * c.W] = 0;  // diagonal 0 of slot 0
   } else {
     d.lused = 1;
-    for (int ci = 0; ci < 3; ++ci) d.ldesc[ci] = make_int4(kAbsent, INT_MIN, 0, 0);
-    d.ldesc[cbi] = make_int4(0, 0, 0, 0);
-    d.ldata[0] = 0;
+    for (int ci = 0; ci < 3; ++ci) c.ldesc[ci] = make_int4(kAbsent, INT_MIN, 0, 0);
+    c.ldesc[cbi] = make_int4(0, 0, 0, 0);
+    c.ldata[0] = 0;
   }
 }
 
 // wavefront_compute_affine. Returns false when the scratch is too small (the pair is
 // retried with a larger arena).
-__device__ bool dir_compute(Dir& d, const Pen& p, int s, int lane) {
-  if (d.leaf && s > d.lmax) return false;
-  const WfRef mx = fetch(d, s - p.x, 0);
-  const WfRef mo = fetch(d, s - p.o - p.e, 0);
-  const WfRef ie = fetch(d, s - p.e, 1);
-  const WfRef de = fetch(d, s - p.e, 2);
+__device__ __noinline__ bool dir_compute(Dir& d, const Pen p, int s, int lane) {
+  const DirCfg c = d.cfg;
+  if (c.leaf && s > c.lmax) return false;
+  const WfRef mx = fetch(c, s - p.x, 0);
+  const WfRef mo = fetch(c, s - p.o - p.e, 0);
+  const WfRef ie = fetch(c, s - p.e, 1);
+  const WfRef de = fetch(c, s - p.e, 2);
   const bool hx = mx.nonnull(), ho = mo.nonnull(), hie = ie.nonnull(), hde = de.nonnull();
   if (!hx && !ho && !hie && !hde) {
     d.num_null += 1;
-    set_desc(d, s, 0, kAbsent, INT_MIN, 0, 0);
-    set_desc(d, s, 1, kAbsent, INT_MIN, 0, 0);
-    set_desc(d, s, 2, kAbsent, INT_MIN, 0, 0);
+    set_desc(c, s, 0, kAbsent, INT_MIN, 0, 0);
+    set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
+    set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
     return true;
   }
   d.num_null = 0;
@@ -178,22 +194,23 @@ __device__ bool dir_compute(Dir& d, const Pen& p, int s, int lane) {
   const int width = hi - lo + 1;
   WfRef om, oi, od;
   int offm = 0, offi = 0, offd = 0;
-  if (!d.leaf) {
-    if (width > d.W) return false;
-    const int slot = s % d.scope;
-    om.base = d.rdata + (size_t)(slot * 3 + 0) * d.W;
-    oi.base = d.rdata + (size_t)(slot * 3 + 1) * d.W;
-    od.base = d.rdata + (size_t)(slot * 3 + 2) * d.W;
+  if (!c.leaf) {
+    if (width > c.W) return false;
+    const int slot = slot_of(c, s);
+    om.base = c.rdata + (size_t)(slot * 3 + 0) * c.W;
+    oi.base = om.base + c.W;
+    od.base = oi.base + c.W;
     om.kbase = oi.kbase = od.kbase = 0;
-    om.mask = oi.mask = od.mask = (uint32_t)d.W - 1u;
+    om.mask = oi.mask = od.mask = (uint32_t)c.W - 1u;
   } else {
     const int need = width * (1 + (ai ? 1 : 0) + (ad ? 1 : 0));
-    if (d.lused + need > d.lcap) return false;
-    offm = d.lused;
+    const int used = d.lused;
+    if (used + need > d.lcap) return false;
+    offm = used;
     offi = offm + width;
     offd = offi + (ai ? width : 0);
-    d.lused += need;
-    om.base = d.ldata + offm; oi.base = d.ldata + offi; od.base = d.ldata + offd;
+    d.lused = used + need;
+    om.base = c.ldata + offm; oi.base = c.ldata + offi; od.base = c.ldata + offd;
     om.kbase = oi.kbase = od.kbase = lo;
     om.mask = oi.mask = od.mask = 0xffffffffu;
   }
@@ -222,36 +239,39 @@ __device__ bool dir_compute(Dir& d, const Pen& p, int s, int lane) {
   ilo = __reduce_min_sync(kFull, ilo); ihi = __reduce_max_sync(kFull, ihi);
   dlo = __reduce_min_sync(kFull, dlo); dhi = __reduce_max_sync(kFull, dhi);
   __syncwarp();
-  if (mlo <= mhi) set_desc(d, s, 0, mlo, mhi, offm, lo); else set_desc(d, s, 0, lo, lo - 1, offm, lo);
-  if (ai) { if (ilo <= ihi) set_desc(d, s, 1, ilo, ihi, offi, lo); else set_desc(d, s, 1, lo, lo - 1, offi, lo); }
-  else set_desc(d, s, 1, kAbsent, INT_MIN, 0, 0);
-  if (ad) { if (dlo <= dhi) set_desc(d, s, 2, dlo, dhi, offd, lo); else set_desc(d, s, 2, lo, lo - 1, offd, lo); }
-  else set_desc(d, s, 2, kAbsent, INT_MIN, 0, 0);
+  if (mlo <= mhi) set_desc(c, s, 0, mlo, mhi, offm, lo); else set_desc(c, s, 0, lo, lo - 1, offm, lo);
+  if (ai) { if (ilo <= ihi) set_desc(c, s, 1, ilo, ihi, offi, lo); else set_desc(c, s, 1, lo, lo - 1, offi, lo); }
+  else set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
+  if (ad) { if (dlo <= dhi) set_desc(c, s, 2, dlo, dhi, offd, lo); else set_desc(c, s, 2, lo, lo - 1, offd, lo); }
+  else set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
   return true;
 }
 
 // wavefront_extend_end2end(_max) + wavefront_termination_end2end. Returns 1 when the
 // direction is finished (end reached or unreachable).
-__device__ int dir_extend(Dir& d, int s, int lane, int* max_ak_out) {
+__device__ __noinline__ int dir_extend(Dir& d, int s, int lane, int* max_ak_out) {
+  const DirCfg c = d.cfg;
   if (max_ak_out) *max_ak_out = 0;
-  const WfRef m = ref_raw(d, s, 0);
+  const WfRef m = ref_raw(c, s, 0);
   if (!m.present()) {
-    if (d.num_null > d.scope) { d.status = ST_END_UNREACHABLE; d.status_score = s; return 1; }
+    if (d.num_null > c.scope) { d.status = ST_END_UNREACHABLE; d.status_score = s; return 1; }
     return 0;
   }
+  const SeqView sv = d.sv;
   int my = 0;
   for (int k = m.lo + lane; k <= m.hi; k += 32) {
     int32_t off = m.at(k);
     if (off == kNull) continue;
-    off += lcp(d.sv, off - k, off);
+    off += lcp(sv, off - k, off);
     m.put(k, off);
     my = max(my, 2 * off - k);
   }
   const int mak = __reduce_max_sync(kFull, my);
   __syncwarp();
-  const int ak = d.sv.tlen - d.sv.plen;
-  const WfRef t = (d.ce == CM) ? m : ref_raw(d, s, comp_index(d.ce));
-  const bool done = (t.lo <= ak && ak <= t.hi) && (t.at(ak) >= d.sv.tlen);
+  const int ak = sv.tlen - sv.plen;
+  const int ce = d.ce;
+  const WfRef t = (ce == CM) ? m : ref_raw(c, s, comp_index(ce));
+  const bool done = (t.lo <= ak && ak <= t.hi) && (t.at(ak) >= sv.tlen);
   if (done) { d.status = ST_END_REACHED; d.status_score = s; d.end_k = ak; return 1; }
   if (max_ak_out) *max_ak_out = mak;
   return 0;
@@ -300,38 +320,40 @@ __device__ void bp_scan(bool is_m, bool fwd, int s0, int s1, const WfRef& w0, co
 }
 
 // wavefront_bialign_overlap (gap-affine part)
-__device__ void overlap(const Dir& d0, const Dir& d1, int s0, int s1, bool fwd, BP& bp, const Pen& p, int lane) {
+__device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s1, bool fwd, BP& bp, const Pen p,
+                                     int lane) {
+  const DirCfg c0 = d0.cfg, c1 = d1.cfg;
   const int plen = d0.sv.plen, tlen = d0.sv.tlen;
-  const WfRef m0 = ref_raw(d0, s0, 0);
+  const WfRef m0 = ref_raw(c0, s0, 0);
   if (!m0.present()) return;
-  const WfRef dd0 = ref_raw(d0, s0, 2);
-  const WfRef ii0 = ref_raw(d0, s0, 1);
+  const WfRef dd0 = ref_raw(c0, s0, 2);
+  const WfRef ii0 = ref_raw(c0, s0, 1);
   for (int i = 0; i < p.scope; ++i) {
     const int si = s1 - i;
     if (si < 0) break;
     if (s0 + si - p.o >= bp.score) continue;
-    const WfRef dd1 = ref_raw(d1, si, 2);
+    const WfRef dd1 = ref_raw(c1, si, 2);
     if (dd0.present() && dd1.present()) bp_scan(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, lane);
-    const WfRef ii1 = ref_raw(d1, si, 1);
+    const WfRef ii1 = ref_raw(c1, si, 1);
     if (ii0.present() && ii1.present()) bp_scan(false, fwd, s0, si, ii0, ii1, plen, tlen, p.o, CI, bp, lane);
     if (s0 + si >= bp.score) continue;
-    const WfRef mm1 = ref_raw(d1, si, 0);
+    const WfRef mm1 = ref_raw(c1, si, 0);
     if (mm1.present()) bp_scan(true, fwd, s0, si, m0, mm1, plen, tlen, p.o, CM, bp, lane);
   }
 }
 
 struct PairSeqs {
   const uint32_t* pf; const uint32_t* tf; const uint32_t* pr; const uint32_t* tr;
-  int plen, tlen, bits;
+  int plen, tlen, bshift;
 };
 
 __device__ __forceinline__ SeqView fwd_view(const PairSeqs& q, int pb, int pe, int tb, int te) {
-  SeqView v; v.pw = q.pf; v.tw = q.tf; v.p0 = pb; v.t0 = tb; v.plen = pe - pb; v.tlen = te - tb; v.bits = q.bits;
+  SeqView v; v.pw = q.pf; v.tw = q.tf; v.p0 = pb; v.t0 = tb; v.plen = pe - pb; v.tlen = te - tb; v.bshift = q.bshift;
   return v;
 }
 __device__ __forceinline__ SeqView rev_view(const PairSeqs& q, int pb, int pe, int tb, int te) {
   SeqView v; v.pw = q.pr; v.tw = q.tr; v.p0 = q.plen - pe; v.t0 = q.tlen - te;
-  v.plen = pe - pb; v.tlen = te - tb; v.bits = q.bits;
+  v.plen = pe - pb; v.tlen = te - tb; v.bshift = q.bshift;
   return v;
 }
 
@@ -343,8 +365,8 @@ __device__ __forceinline__ int score_guard(const Pen& p, int plen, int tlen) {
 }
 
 // wavefront_bialign_find_breakpoint
-__device__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, int pb, int pe, int tb, int te,
-                               int cb, int ce, const Pen& p, int max_steps, BP& bp, int lane, bool& overflow) {
+__device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, int pb, int pe, int tb, int te,
+                                            int cb, int ce, const Pen p, int max_steps, BP& bp, int lane, bool& overflow) {
   dir_init(F, fwd_view(q, pb, pe, tb, te), cb, ce);
   dir_init(R, rev_view(q, pb, pe, tb, te), ce, cb);
   __syncwarp();
@@ -419,7 +441,7 @@ struct RunOut {
 
 // wavefront_backtrace_affine: packed (offset<<4)|type source of one step, or the
 // unshifted null when the source is absent or out of range.
-__device__ __forceinline__ long long bt_src(const Dir& B, int score, int ci, int kk, int add, int type) {
+__device__ __forceinline__ long long bt_src(const DirCfg& B, int score, int ci, int kk, int add, int type) {
   if (score < 0) return (long long)kNull;
   const WfRef w = ref_raw(B, score, ci);
   if (w.lo <= kk && kk <= w.hi) return (long long)(w.at(kk) + add) * 16LL + type;
@@ -427,8 +449,8 @@ __device__ __forceinline__ long long bt_src(const Dir& B, int score, int ci, int
 }
 
 // Leaf: wavefront_bialign_base -> unialign -> backtrace. Appends the leaf's ops to out.
-__device__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe, int tb, int te, int cb, int ce,
-                          const Pen& p, int max_steps, RunOut& out, uint32_t* lruns, int lruns_cap,
+__device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe, int tb, int te, int cb, int ce,
+                                       const Pen p, int max_steps, RunOut& out, uint32_t* lruns, int lruns_cap,
                           int lane, int* max_leaf_score) {
   dir_init(B, fwd_view(q, pb, pe, tb, te), cb, ce);
   __syncwarp();
@@ -443,6 +465,7 @@ __device__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe, int tb, int
   }
   if (*max_leaf_score < s) *max_leaf_score = s;
   if (B.status != ST_END_REACHED) return WFG_ST_UNATTAINABLE;
+  const DirCfg bc = B.cfg;
   // Backtrace from (end_k, tlen) in component ce; runs are produced end -> begin.
   const int plen = B.sv.plen, tlen = B.sv.tlen;
   int nrev = 0; int rop = -1, rlen = 0; bool rover = false;
@@ -465,22 +488,22 @@ __device__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe, int tb, int
     const int mm = score - p.x, go = score - p.o - p.e, ge = score - p.e;
     long long max_all;
     if (matrix == CM) {
-      const long long mis = bt_src(B, mm, 0, k, 1, BT_M);
-      const long long io = bt_src(B, go, 0, k - 1, 1, BT_I_OPEN);
-      const long long ix = bt_src(B, ge, 1, k - 1, 1, BT_I_EXT);
-      const long long dop = bt_src(B, go, 0, k + 1, 0, BT_D_OPEN);
-      const long long dx = bt_src(B, ge, 2, k + 1, 0, BT_D_EXT);
+      const long long mis = bt_src(bc, mm, 0, k, 1, BT_M);
+      const long long io = bt_src(bc, go, 0, k - 1, 1, BT_I_OPEN);
+      const long long ix = bt_src(bc, ge, 1, k - 1, 1, BT_I_EXT);
+      const long long dop = bt_src(bc, go, 0, k + 1, 0, BT_D_OPEN);
+      const long long dx = bt_src(bc, ge, 2, k + 1, 0, BT_D_EXT);
       const long long mi = io >= ix ? io : ix;
       const long long md = dop >= dx ? dop : dx;
       const long long mid = mi >= md ? mi : md;
       max_all = mis >= mid ? mis : mid;
     } else if (matrix == CI) {
-      const long long io = bt_src(B, go, 0, k - 1, 1, BT_I_OPEN);
-      const long long ix = bt_src(B, ge, 1, k - 1, 1, BT_I_EXT);
+      const long long io = bt_src(bc, go, 0, k - 1, 1, BT_I_OPEN);
+      const long long ix = bt_src(bc, ge, 1, k - 1, 1, BT_I_EXT);
       max_all = io >= ix ? io : ix;
     } else {
-      const long long dop = bt_src(B, go, 0, k + 1, 0, BT_D_OPEN);
-      const long long dx = bt_src(B, ge, 2, k + 1, 0, BT_D_EXT);
+      const long long dop = bt_src(bc, go, 0, k + 1, 0, BT_D_OPEN);
+      const long long dx = bt_src(bc, ge, 2, k + 1, 0, BT_D_EXT);
       max_all = dop >= dx ? dop : dx;
     }
     if (max_all < 0) break;
@@ -540,7 +563,7 @@ __device__ __forceinline__ int classic_score(int match_o, int plen, int tlen, in
 }  // namespace
 
 template <int WPB>
-__global__ void __launch_bounds__(WPB * 32) biwfa_persistent_kernel(KernelParams P) {
+__global__ void __launch_bounds__(WPB * 32, kMinBlocksPerSM) biwfa_persistent_kernel(KernelParams P) {
   __shared__ Dir s_dir[WPB][3];
   __shared__ int2 s_rdesc[WPB][2][kMaxScope * 3];
   const int lane = threadIdx.x & 31;
@@ -560,10 +583,18 @@ __global__ void __launch_bounds__(WPB * 32) biwfa_persistent_kernel(KernelParams
   Dir& R = s_dir[wib][1];
   Dir& B = s_dir[wib][2];
   const size_t ring_dir = (size_t)P.scope * 3 * P.ring_w;
-  F.leaf = 0; F.scope = P.scope; F.rdesc = s_rdesc[wib][0]; F.rdata = ring; F.W = P.ring_w;
-  R.leaf = 0; R.scope = P.scope; R.rdesc = s_rdesc[wib][1]; R.rdata = ring + ring_dir; R.W = P.ring_w;
-  B.leaf = 1; B.scope = P.scope; B.ldesc = ldesc; B.ldata = ldata; B.lcap = P.leaf_words; B.lmax = P.leaf_max_score;
-  B.lused = 0;
+  const uint32_t magic = (uint32_t)(0xffffffffu / (uint32_t)P.scope) + 1u;
+  DirCfg fc{};
+  fc.leaf = 0; fc.scope = P.scope; fc.magic = magic; fc.W = P.ring_w; fc.lmax = 0;
+  fc.rdesc = s_rdesc[wib][0]; fc.rdata = ring;
+  DirCfg rc = fc;
+  rc.rdesc = s_rdesc[wib][1]; rc.rdata = ring + ring_dir;
+  DirCfg bcfg{};
+  bcfg.leaf = 1; bcfg.scope = P.scope; bcfg.magic = magic; bcfg.W = 0; bcfg.lmax = P.leaf_max_score;
+  bcfg.ldesc = ldesc; bcfg.ldata = ldata;
+  F.cfg = fc; R.cfg = rc; B.cfg = bcfg;
+  F.lcap = R.lcap = 0; F.lused = R.lused = 0;
+  B.lcap = P.leaf_words; B.lused = 0;
   __syncwarp();
   const Pen pen = {P.x, P.o, P.e, P.scope};
 
@@ -581,7 +612,7 @@ __global__ void __launch_bounds__(WPB * 32) biwfa_persistent_kernel(KernelParams
     q.tf = q.pf + pd.pw_len;
     q.pr = q.tf + pd.tw_len;
     q.tr = q.pr + pd.pw_len;
-    q.plen = pd.plen; q.tlen = pd.tlen; q.bits = pd.bits;
+    q.plen = pd.plen; q.tlen = pd.tlen; q.bshift = (pd.bits == 2) ? 1 : 3;
     int status = ST_OK;
     int score = 0;
     int nsteps = 0, max_leaf = -1, max_depth = 0;
