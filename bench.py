@@ -41,6 +41,7 @@ WORKLOADS = {
 }
 PENALTIES = (0, 4, 6, 2)
 SEED = 20251203
+TRAIN_SEED = 99991  # held-out seed of the predictor's training pairs
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -182,16 +183,15 @@ def cpu_baseline(batch, sample_seconds: float = 12.0, threads: int | None = None
     n = batch.n
     rng = np.random.default_rng(99)
     order = rng.permutation(n)
-    # calibrate on a small sample, then size the sample to ~sample_seconds of wall time
-    m = min(n, max(threads * 4, 64))
-    sub = batch.subset(order[:m])
-    secs, _, _ = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen, PENALTIES,
-                                           threads=threads)
-    per_pair = max(secs, 1e-6) / m
-    m2 = int(min(n, max(m, sample_seconds / per_pair)))
-    sub = batch.subset(order[:m2])
-    secs, scores, status = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen,
-                                                     PENALTIES, threads=threads)
+    # grow the sample until it takes about sample_seconds of wall time (or covers the batch)
+    m2 = min(n, max(threads * 16, 256))
+    while True:
+        sub = batch.subset(order[:m2])
+        secs, scores, status = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen,
+                                                         PENALTIES, threads=threads)
+        if secs >= 0.5 * sample_seconds or m2 >= n:
+            break
+        m2 = int(min(n, m2 * max(2.0, min(8.0, sample_seconds / max(secs, 1e-3)))))
     cells = float((sub.plen.astype(np.float64) * sub.tlen).sum())
     return {"value": m2 / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
             "sample": f"{m2} pairs drawn uniformly (seed 99) from the same batch; {secs:.2f} s wall",
@@ -245,31 +245,39 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
-    import biwfa_gpu_pii2025_gb300 as pkg
-    from biwfa_gpu_pii2025_gb300 import _capi
-    rank, world, local = dist_env()
-    dist = Dist(world)
-    wl = args.workload
-    name, n_full = WORKLOADS[wl]
-    n = args.pairs or n_full
-    batch = make_batch(wl, n, rank)
-    al = pkg.BatchAligner(local if world > 1 else 0)
-    sched = _capi.SCHED_PLAIN
-    sched_name = "plain (length-sorted, one arena size)"
+def train_predictor(pkg, al, wl: int, n_train: int, rank: int):
+    """The learned scheduler's model: trained on the GPU on n_train pairs of the same generator
+    with a held-out seed, scored by the plain method (score-only); the policy (which pairs get
+    several warps and shared-memory rings) is then autotuned on a held-out slice."""
+    t0 = time.perf_counter()
+    train = pkg.PairBatch.generate(wl, n_train, TRAIN_SEED + 7919 * rank)
+    al.upload(train)
+    al.run(PENALTIES, score_only=True)
+    scores = al.fetch().scores
+    pred = pkg.ScorePredictor(al, seed=17)
+    losses = pred.train(-scores, epochs=20, batch_rows=4096, lr=3e-3, seed=5)
+    train_s = time.perf_counter() - t0
+    # the autotuner measures on a held-out slice of the same generator (another seed)
+    tune_n = min(n_train, 60_000)
+    al.upload(pkg.PairBatch.generate(wl, tune_n, TRAIN_SEED + 1 + 7919 * rank))
+    pred.attach()
+    tuned = al.autotune_learned_policy(PENALTIES)
+    info = {"train_pairs": n_train, "train_seed": TRAIN_SEED, "epochs": 20, "final_loss": float(losses[-1]),
+            "first_loss": float(losses[0]), "train_s": train_s, "policy": tuned}
+    return pred, info
 
-    # ---- device-resident throughput (value)
-    al.upload(batch)
-    for _ in range(args.warmup):
+
+def time_path(al, sched, steps: int, warmup: int, dist, clocks=None):
+    for _ in range(warmup):
         al.flush_l2(L2_FLUSH_BYTES)
         al.run(PENALTIES, sched=sched)
         al.synchronize()
     step_ms, kernel_ms, launches = [], [], 0
-    clocks = ClockSampler(local if world > 1 else 0)
-    clocks.start()
+    if clocks:
+        clocks.start()
     dist.barrier()
     al.synchronize()
-    for _ in range(args.steps):
+    for _ in range(steps):
         al.flush_l2(L2_FLUSH_BYTES)
         al.synchronize()
         t0 = time.perf_counter()
@@ -280,11 +288,42 @@ def run_ours(args):
         kernel_ms.append(st.kernel_ms)
         launches += st.launches
     dist.barrier()
-    clk = clocks.stop()
+    clk = clocks.stop() if clocks else None
+    return step_ms, kernel_ms, launches, clk
+
+
+def run_ours(args):
+    import biwfa_gpu_pii2025_gb300 as pkg
+    from biwfa_gpu_pii2025_gb300 import _capi
+    rank, world, local = dist_env()
+    dist = Dist(world)
+    wl = args.workload
+    name, n_full = WORKLOADS[wl]
+    n = args.pairs or n_full
+    al = pkg.BatchAligner(local if world > 1 else 0)
+    learned = not args.plain_only
+    pred, learn_info = None, None
+    if learned:
+        pred, learn_info = train_predictor(pkg, al, wl, min(200_000, max(n, 2000)), rank)
+    batch = make_batch(wl, n, rank)
+    al.upload(batch)
+    if learned:
+        pred.attach()
+    # ---- plain length-sorted path (the comparison), then the learned-binned path (value)
+    plain_ms, plain_kernel_ms, _, _ = time_path(al, _capi.SCHED_PLAIN, args.steps, args.warmup, dist)
+    plain_res = al.fetch()
+    sched = _capi.SCHED_LEARNED if learned else _capi.SCHED_PLAIN
+    sched_name = ("learned-binned (MLP score prediction; autotuned warps-per-pair and shared-memory rings)"
+                  if learned else "plain (length-sorted, one arena size)")
+    step_ms, kernel_ms, launches, clk = time_path(al, sched, args.steps, args.warmup, dist,
+                                                  ClockSampler(local if world > 1 else 0))
     res = al.fetch()
     ok = int((res.status == 0).sum())
+    same_as_plain = bool(np.array_equal(res.scores, plain_res.scores) and np.array_equal(res.status, plain_res.status)
+                         and np.array_equal(res.run_len, plain_res.run_len))
     total_runs = int(res.runs.shape[0])
     t_step = dist.max(statistics.mean(step_ms))
+    t_plain = dist.max(statistics.mean(plain_ms))
     pairs_all = dist.sum(float(n))
     value = pairs_all / (t_step / 1e3)
     cells = float((batch.plen.astype(np.float64) * batch.tlen).sum())
@@ -325,6 +364,10 @@ def run_ours(args):
                        "sched": sched_name, "l2": "flushed before every step (512 MiB write)",
                        "parallelism": f"{world} GPU(s), independent pair shards"},
             "gcups": gcups, "pairs_ok": ok,
+            "plain_value": pairs_all / (t_plain / 1e3), "plain_ms_per_step": t_plain,
+            "learned_over_plain": (t_plain / t_step) if learned else None,
+            "results_identical_to_plain": same_as_plain,
+            "learned": learn_info,
             "e2e": {"value": dist.sum(float(n)) / (e2e_t / 1e3), "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t, "matches_device_run": e2e_ok},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -353,6 +396,7 @@ def main():
     ap.add_argument("--workload", type=int, default=5, choices=sorted(WORKLOADS))
     ap.add_argument("--pairs", type=int, default=0, help="override the workload's pair count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-only", action="store_true", help="time only the plain length-sorted path")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -136,6 +136,9 @@ SIGNATURES = {
                                  _i64p, _ip, _ip, _ip, _i64p, _ip, _u32p, C.c_int64, _i64p]),
     "wfg_get_stats": (C.c_int, [C.c_void_p, P(Stats)]),
     "wfg_set_arena_limits": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "wfg_set_exec_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "wfg_set_learned_policy": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_float]),
+    "wfg_autotune_learned_policy": (C.c_int, [C.c_void_p, P(Config), P(C.c_float), P(C.c_float), _ip, _ip]),
     "wfg_flush_l2": (C.c_int, [C.c_void_p, C.c_int64]),
     "wfg_synchronize": (C.c_int, [C.c_void_p]),
     "wfg_host_alloc": (C.c_void_p, [C.c_int64]),
@@ -143,6 +146,17 @@ SIGNATURES = {
     "wfg_align_noalloc": (C.c_int, [P(Config), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                     C.c_void_p]),
+    "wfg_model_param_count": (C.c_int, []),
+    "wfg_model_create": (C.c_void_p, [C.c_void_p, C.c_uint64]),
+    "wfg_model_destroy": (None, [C.c_void_p]),
+    "wfg_model_get_params": (C.c_int, [C.c_void_p, P(C.c_float)]),
+    "wfg_model_set_params": (C.c_int, [C.c_void_p, P(C.c_float)]),
+    "wfg_features": (C.c_int, [C.c_void_p, P(C.c_uint16)]),
+    "wfg_model_train": (C.c_int, [C.c_void_p, C.c_void_p, _ip, C.c_int, C.c_int, C.c_float, C.c_uint64,
+                                  P(C.c_float)]),
+    "wfg_model_gradient": (C.c_int, [C.c_void_p, C.c_void_p, P(C.c_float), P(C.c_float), P(C.c_float)]),
+    "wfg_model_predict": (C.c_int, [C.c_void_p, C.c_void_p, P(C.c_float)]),
+    "wfg_set_model": (C.c_int, [C.c_void_p, C.c_void_p]),
     "wfg_generate": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.c_void_p, _i64p, _i64p, _ip, _i64p, _ip]),
 }
 

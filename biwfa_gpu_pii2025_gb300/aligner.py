@@ -175,6 +175,23 @@ class BatchAligner:
     def set_arena_limits(self, ring_w: int = 0, leaf_words: int = 0):
         self._check(self.lib.wfg_set_arena_limits(self.ctx, ring_w, leaf_words), "wfg_set_arena_limits")
 
+    def set_exec_shape(self, group_warps: int = 1, ring_in_smem: bool = False):
+        self._check(self.lib.wfg_set_exec_shape(self.ctx, group_warps, 1 if ring_in_smem else 0),
+                    "wfg_set_exec_shape")
+
+    def set_learned_policy(self, wide_threshold=1200.0, wide_warps=8, wide_smem=True, ring_margin=1.4):
+        self._check(self.lib.wfg_set_learned_policy(self.ctx, wide_threshold, wide_warps, 1 if wide_smem else 0,
+                                                    ring_margin), "wfg_set_learned_policy")
+
+    def autotune_learned_policy(self, penalties=(0, 4, 6, 2)):
+        """Measure the learned-schedule policies on the resident batch; keeps and returns the best."""
+        cfg = self.config(penalties, False, 0)
+        ms, thr = C.c_float(0), C.c_float(0)
+        gw, sm = C.c_int(0), C.c_int(0)
+        self._check(self.lib.wfg_autotune_learned_policy(self.ctx, C.byref(cfg), C.byref(ms), C.byref(thr),
+                                                         C.byref(gw), C.byref(sm)), "wfg_autotune_learned_policy")
+        return {"ms": ms.value, "wide_threshold": thr.value, "wide_warps": gw.value, "wide_smem": bool(sm.value)}
+
     def set_predictions(self, pred: np.ndarray):
         pred = np.ascontiguousarray(pred, np.float32)
         self._check(self.lib.wfg_set_predictions(self.ctx, pred.ctypes.data_as(C.POINTER(C.c_float))),
@@ -229,6 +246,78 @@ class BatchAligner:
         s = _capi.Stats()
         self._check(self.lib.wfg_get_stats(self.ctx, C.byref(s)), "wfg_get_stats")
         return s
+
+
+class ScorePredictor:
+    """The learned scheduler's score model (wfg_model_t) on a BatchAligner's device.
+
+    Features, training (forward/backward/Adam kernels, one CUDA-graph per epoch) and
+    inference all run in libbiwfa_gb300.so on the batch resident in the aligner."""
+
+    def __init__(self, aligner: BatchAligner, seed: int = 1):
+        self.al = aligner
+        self.lib = aligner.lib
+        self.model = self.lib.wfg_model_create(aligner.ctx, seed)
+        if not self.model:
+            raise RuntimeError("wfg_model_create failed")
+        self.nparams = self.lib.wfg_model_param_count()
+
+    def close(self):
+        if self.model:
+            self.lib.wfg_set_model(self.al.ctx, None)
+            self.lib.wfg_model_destroy(self.model)
+            self.model = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.nparams, np.float32)
+        self.al._check(self.lib.wfg_model_get_params(self.model, p.ctypes.data_as(C.POINTER(C.c_float))),
+                       "wfg_model_get_params")
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        self.al._check(self.lib.wfg_model_set_params(self.model, p.ctypes.data_as(C.POINTER(C.c_float))),
+                       "wfg_model_set_params")
+
+    def features(self) -> np.ndarray:
+        """bf16 bit patterns of the resident batch's features (n x 32, uint16)."""
+        f = np.empty((self.al.n, 32), np.uint16)
+        self.al._check(self.lib.wfg_features(self.al.ctx, f.ctypes.data_as(C.POINTER(C.c_uint16))),
+                       "wfg_features")
+        return f
+
+    def train(self, target_scores: np.ndarray, epochs=20, batch_rows=2048, lr=2e-3, seed=7) -> np.ndarray:
+        t = np.ascontiguousarray(target_scores, np.int32)
+        losses = np.zeros(max(epochs, 1), np.float32)
+        st = self.lib.wfg_model_train(self.model, self.al.ctx, _ptr(t, _ip), epochs, batch_rows, lr, seed,
+                                      losses.ctypes.data_as(C.POINTER(C.c_float)))
+        self.al._check(st, "wfg_model_train")
+        return losses[:epochs]
+
+    def gradient(self, log_targets: np.ndarray):
+        t = np.ascontiguousarray(log_targets, np.float32)
+        g = np.empty(self.nparams, np.float32)
+        loss = C.c_float(0)
+        st = self.lib.wfg_model_gradient(self.model, self.al.ctx, t.ctypes.data_as(C.POINTER(C.c_float)),
+                                         g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss))
+        self.al._check(st, "wfg_model_gradient")
+        return float(loss.value), g
+
+    def predict(self) -> np.ndarray:
+        out = np.empty(self.al.n, np.float32)
+        self.al._check(self.lib.wfg_model_predict(self.model, self.al.ctx, out.ctypes.data_as(C.POINTER(C.c_float))),
+                       "wfg_model_predict")
+        return out
+
+    def attach(self):
+        """Use this model for SCHED_LEARNED runs of the aligner."""
+        self.al._check(self.lib.wfg_set_model(self.al.ctx, self.model), "wfg_set_model")
 
 
 class WavefrontAligner:

@@ -22,7 +22,8 @@ LIB = PKG / "libbiwfa_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
-SOURCES = ["biwfa_kernel.cu", "wfg_runtime.cpp", "wfa2_compat.cpp", "datagen.cpp", "noalloc.cu"]
+SOURCES = ["biwfa_kernel.cu", "wfg_runtime.cpp", "wfa2_compat.cpp", "datagen.cpp", "noalloc.cu", "mlp_kernel.cu",
+           "wfg_model.cpp", "autotune.cpp"]
 
 
 def nvcc_path() -> str:
@@ -35,7 +36,7 @@ def nvcc_path() -> str:
 def _compile(src: str) -> Path:
     out = BUILD / (Path(src).stem + ".o")
     srcp = CSRC / src
-    deps = [srcp, CSRC / "wfg_internal.h", ROOT / "include" / "wfa_gpu.h"]
+    deps = [srcp, CSRC / "wfg_internal.h", CSRC / "wfg_context.h", ROOT / "include" / "wfa_gpu.h"]
     if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps if d.exists()):
         return out
     lang = [] if src.endswith(".cu") else ["-x", "cu"] if src.endswith("_kernel.cpp") else []

@@ -1,9 +1,9 @@
 // GB300 (sm_103a) bidirectional WFA, gap-affine, end-to-end: score + CIGAR on the device.
 //
-// One warp owns one pair at a time; warps pull pair indices from a global work queue
-// (one atomicAdd per pair) so a single persistent launch drains a whole uneven batch.
-// Within a pair, lanes split the diagonals of every wavefront; all control state
-// (scores, breakpoints, recursion) is warp-uniform.
+// A group of G warps (G = 1 for most pairs, 4 or 8 for wide ones) owns one pair at a time;
+// groups pull pair indices from a global work queue (one atomicAdd per pair) so a single
+// persistent launch drains a whole uneven batch. Within a pair, threads split the diagonals
+// of every wavefront; all control state (scores, breakpoints, recursion) is group-uniform.
 //
 // Semantics follow WFA2-lib v2.3 exactly (paths relative to WFA2-lib/):
 //   compute      wavefront/wavefront_compute_affine.c:44-86, 229-260; wavefront_compute.c:40-104, 306-632
@@ -92,6 +92,50 @@ __device__ __forceinline__ int lcp(const SeqView& s, int v, int h) {
   return min(n, maxn);
 }
 
+// A group of G warps that owns one pair. G == 1: warp-synchronous; G > 1: the warps meet
+// at named barrier `bar` (one per group in a block) and reduce through `red` (shared memory,
+// >= 8*G + 4 ints).
+template <int G>
+struct Grp {
+  int tid;      // 0 .. 32*G-1
+  int bar;
+  int* red;
+  __device__ __forceinline__ int lane() const { return tid & 31; }
+  __device__ __forceinline__ int warp() const { return tid >> 5; }
+  __device__ __forceinline__ void sync() const {
+    if (G == 1) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(G * 32) : "memory");
+  }
+  // min/max of up to 6 values at once (slot j of each warp in red[warp*8 + j])
+  template <int N>
+  __device__ __forceinline__ void minmax(int (&v)[N], const bool (&is_max)[N]) const {
+    #pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = is_max[j] ? __reduce_max_sync(kFull, v[j]) : __reduce_min_sync(kFull, v[j]);
+    if (G == 1) return;
+    if (lane() == 0) {
+      #pragma unroll
+      for (int j = 0; j < N; ++j) red[warp() * 8 + j] = v[j];
+    }
+    sync();
+    #pragma unroll
+    for (int j = 0; j < N; ++j) {
+      int r = red[j];
+      for (int w = 1; w < G; ++w) r = is_max[j] ? max(r, red[w * 8 + j]) : min(r, red[w * 8 + j]);
+      v[j] = r;
+    }
+    sync();
+  }
+  // value of thread `src_tid` to every thread of the group
+  __device__ __forceinline__ int bcast(int v, int src_tid) const {
+    if (G == 1) return __shfl_sync(kFull, v, src_tid);
+    if (tid == src_tid) red[8 * G] = v;
+    sync();
+    const int r = red[8 * G];
+    sync();
+    return r;
+  }
+};
+
 // Storage configuration of one direction, fixed for the kernel's lifetime; functions copy
 // it into registers once per call.
 struct DirCfg {
@@ -99,18 +143,22 @@ struct DirCfg {
   int scope;
   uint32_t magic;    // floor(2^32 / scope) + 1: slot = s - scope * umulhi(s, magic), s < 2^27
   int W;             // ring width (power of two)
+  int nphys;         // physical ring buffers (round-robin over non-null steps)
   int lmax;          // leaf descriptor capacity (scores)
   int2* rdesc;       // ring descriptors [scope*3] (shared memory)
-  int32_t* rdata;    // ring storage [scope*3][W]
+  int* rphys;        // physical buffer of each ring slot [scope] (shared memory)
+  int32_t* rdata;    // ring storage [nphys*3][W]
   int4* ldesc;       // leaf descriptors [(lmax+1)*3] {lo, hi, data_off, kbase}
   int32_t* ldata;
 };
 
 // One direction of WFA over one window (a wavefront_aligner_t in WFA2). Lives in shared
-// memory; every lane updates its fields with identical values.
+// memory; every thread of the group updates its fields with identical values. A field that
+// a call reads is written by that call only after a group barrier (G > 1).
 struct Dir {
   DirCfg cfg;
   int lcap, lused;
+  int next_phys;
   SeqView sv;
   int cb, ce;
   int num_null, status, status_score, end_k;
@@ -127,7 +175,7 @@ __device__ __forceinline__ WfRef ref_raw(const DirCfg& c, int score, int ci) {
     const int slot = slot_of(c, score);
     const int2 ds = c.rdesc[slot * 3 + ci];
     r.lo = ds.x; r.hi = ds.y;
-    r.base = c.rdata + (size_t)(slot * 3 + ci) * (size_t)c.W;
+    r.base = c.rdata + (size_t)(c.rphys[slot] * 3 + ci) * (size_t)c.W;
     r.kbase = 0; r.mask = (uint32_t)c.W - 1u;
   } else {
     if (score > c.lmax) return absent_ref();
@@ -149,7 +197,8 @@ __device__ __forceinline__ void set_desc(const DirCfg& c, int score, int ci, int
   else c.ldesc[score * 3 + ci] = make_int4(lo, hi, data_off, kbase);
 }
 
-// wavefront_aligner_init / init_wf (wavefront/wavefront_aligner.c:251-417)
+// wavefront_aligner_init / init_wf (wavefront/wavefront_aligner.c:251-417). The caller
+// has passed a group barrier since the last read of d.
 __device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
   const DirCfg c = d.cfg;
   d.sv = sv; d.cb = cb; d.ce = ce;
@@ -157,8 +206,10 @@ __device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
   const int cbi = comp_index(cb);
   if (!c.leaf) {
     for (int i = 0; i < c.scope * 3; ++i) c.rdesc[i] = make_int2(kAbsent, INT_MIN);
+    for (int i = 0; i < c.scope; ++i) c.rphys[i] = 0;
     c.rdesc[cbi] = make_int2(0, 0);
-    c.rdata[(size_t)cbi * c.W] = 0;  // diagonal 0 of slot 0
+    c.rdata[(size_t)cbi * c.W] = 0;  // diagonal 0 of score 0 (physical buffer 0)
+    d.next_phys = 1 % c.nphys;
   } else {
     d.lused = 1;
     for (int ci = 0; ci < 3; ++ci) c.ldesc[ci] = make_int4(kAbsent, INT_MIN, 0, 0);
@@ -169,8 +220,11 @@ __device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
 
 // wavefront_compute_affine. Returns false when the scratch is too small (the pair is
 // retried with a larger arena).
-__device__ __noinline__ bool dir_compute(Dir& d, const Pen p, int s, int lane) {
+template <int G>
+__device__ __noinline__ bool dir_compute(Dir& d, const Pen p, int s, const Grp<G> g) {
   const DirCfg c = d.cfg;
+  const int nn = d.num_null, used = d.lused, nphys = d.next_phys;
+  const uint32_t tl = (uint32_t)d.sv.tlen, pl = (uint32_t)d.sv.plen;
   if (c.leaf && s > c.lmax) return false;
   const WfRef mx = fetch(c, s - p.x, 0);
   const WfRef mo = fetch(c, s - p.o - p.e, 0);
@@ -178,13 +232,13 @@ __device__ __noinline__ bool dir_compute(Dir& d, const Pen p, int s, int lane) {
   const WfRef de = fetch(c, s - p.e, 2);
   const bool hx = mx.nonnull(), ho = mo.nonnull(), hie = ie.nonnull(), hde = de.nonnull();
   if (!hx && !ho && !hie && !hde) {
-    d.num_null += 1;
+    if (G > 1) g.sync();
+    d.num_null = nn + 1;
     set_desc(c, s, 0, kAbsent, INT_MIN, 0, 0);
     set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
     set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
     return true;
   }
-  d.num_null = 0;
   // A missing input is the shared null wavefront (lo = 1, hi = -1).
   int lo = hx ? mx.lo : 1, hi = hx ? mx.hi : -1;
   lo = min(lo, (ho ? mo.lo : 1) - 1);   hi = max(hi, (ho ? mo.hi : -1) + 1);
@@ -193,63 +247,62 @@ __device__ __noinline__ bool dir_compute(Dir& d, const Pen p, int s, int lane) {
   const bool ai = ho || hie, ad = ho || hde;
   const int width = hi - lo + 1;
   WfRef om, oi, od;
-  int offm = 0, offi = 0, offd = 0;
+  int offm = 0, offi = 0, offd = 0, need = 0;
   if (!c.leaf) {
     if (width > c.W) return false;
-    const int slot = slot_of(c, s);
-    om.base = c.rdata + (size_t)(slot * 3 + 0) * c.W;
+    om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
     oi.base = om.base + c.W;
     od.base = oi.base + c.W;
     om.kbase = oi.kbase = od.kbase = 0;
     om.mask = oi.mask = od.mask = (uint32_t)c.W - 1u;
   } else {
-    const int need = width * (1 + (ai ? 1 : 0) + (ad ? 1 : 0));
-    const int used = d.lused;
+    need = width * (1 + (ai ? 1 : 0) + (ad ? 1 : 0));
     if (used + need > d.lcap) return false;
     offm = used;
     offi = offm + width;
     offd = offi + (ai ? width : 0);
-    d.lused = used + need;
     om.base = c.ldata + offm; oi.base = c.ldata + offi; od.base = c.ldata + offd;
     om.kbase = oi.kbase = od.kbase = lo;
     om.mask = oi.mask = od.mask = 0xffffffffu;
   }
-  const uint32_t tl = (uint32_t)d.sv.tlen, pl = (uint32_t)d.sv.plen;
-  int mlo = INT_MAX, mhi = INT_MIN, ilo = INT_MAX, ihi = INT_MIN, dlo = INT_MAX, dhi = INT_MIN;
-  for (int k = lo + lane; k <= hi; k += 32) {
+  int r[6] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};  // M, I, D trimmed lo/hi
+  for (int k = lo + g.tid; k <= hi; k += 32 * G) {
     const int32_t ins = max(mo.get(k - 1), ie.get(k - 1)) + 1;
     const int32_t del = max(mo.get(k + 1), de.get(k + 1));
     const int32_t mis = mx.get(k) + 1;
     int32_t m = max(del, max(mis, ins));
     if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
     om.put(k, m);
-    if (m != kNull) { mlo = min(mlo, k); mhi = max(mhi, k); }
+    if (m != kNull) { r[0] = min(r[0], k); r[1] = max(r[1], k); }
     if (ai) {
       oi.put(k, ins);
-      if ((uint32_t)ins <= tl && (uint32_t)(ins - k) <= pl) { ilo = min(ilo, k); ihi = max(ihi, k); }
+      if ((uint32_t)ins <= tl && (uint32_t)(ins - k) <= pl) { r[2] = min(r[2], k); r[3] = max(r[3], k); }
     }
     if (ad) {
       od.put(k, del);
-      if ((uint32_t)del <= tl && (uint32_t)(del - k) <= pl) { dlo = min(dlo, k); dhi = max(dhi, k); }
+      if ((uint32_t)del <= tl && (uint32_t)(del - k) <= pl) { r[4] = min(r[4], k); r[5] = max(r[5], k); }
     }
   }
   // Trim both ends of every output (wavefront_compute_trim_ends): the surviving range is
   // [min in-bounds k, max in-bounds k]; none in bounds leaves a null wavefront.
-  mlo = __reduce_min_sync(kFull, mlo); mhi = __reduce_max_sync(kFull, mhi);
-  ilo = __reduce_min_sync(kFull, ilo); ihi = __reduce_max_sync(kFull, ihi);
-  dlo = __reduce_min_sync(kFull, dlo); dhi = __reduce_max_sync(kFull, dhi);
-  __syncwarp();
-  if (mlo <= mhi) set_desc(c, s, 0, mlo, mhi, offm, lo); else set_desc(c, s, 0, lo, lo - 1, offm, lo);
-  if (ai) { if (ilo <= ihi) set_desc(c, s, 1, ilo, ihi, offi, lo); else set_desc(c, s, 1, lo, lo - 1, offi, lo); }
+  const bool mm[6] = {false, true, false, true, false, true};
+  g.minmax(r, mm);
+  g.sync();
+  d.num_null = 0;
+  if (c.leaf) d.lused = used + need;
+  else { c.rphys[slot_of(c, s)] = nphys; d.next_phys = (nphys + 1 == c.nphys) ? 0 : nphys + 1; }
+  if (r[0] <= r[1]) set_desc(c, s, 0, r[0], r[1], offm, lo); else set_desc(c, s, 0, lo, lo - 1, offm, lo);
+  if (ai) { if (r[2] <= r[3]) set_desc(c, s, 1, r[2], r[3], offi, lo); else set_desc(c, s, 1, lo, lo - 1, offi, lo); }
   else set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
-  if (ad) { if (dlo <= dhi) set_desc(c, s, 2, dlo, dhi, offd, lo); else set_desc(c, s, 2, lo, lo - 1, offd, lo); }
+  if (ad) { if (r[4] <= r[5]) set_desc(c, s, 2, r[4], r[5], offd, lo); else set_desc(c, s, 2, lo, lo - 1, offd, lo); }
   else set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
   return true;
 }
 
 // wavefront_extend_end2end(_max) + wavefront_termination_end2end. Returns 1 when the
 // direction is finished (end reached or unreachable).
-__device__ __noinline__ int dir_extend(Dir& d, int s, int lane, int* max_ak_out) {
+template <int G>
+__device__ __noinline__ int dir_extend(Dir& d, int s, const Grp<G> g, int* max_ak_out) {
   const DirCfg c = d.cfg;
   if (max_ak_out) *max_ak_out = 0;
   const WfRef m = ref_raw(c, s, 0);
@@ -258,39 +311,145 @@ __device__ __noinline__ int dir_extend(Dir& d, int s, int lane, int* max_ak_out)
     return 0;
   }
   const SeqView sv = d.sv;
-  int my = 0;
-  for (int k = m.lo + lane; k <= m.hi; k += 32) {
+  const int ce = d.ce;
+  int my[1] = {0};
+  for (int k = m.lo + g.tid; k <= m.hi; k += 32 * G) {
     int32_t off = m.at(k);
     if (off == kNull) continue;
     off += lcp(sv, off - k, off);
     m.put(k, off);
-    my = max(my, 2 * off - k);
+    my[0] = max(my[0], 2 * off - k);
   }
-  const int mak = __reduce_max_sync(kFull, my);
-  __syncwarp();
+  const bool mx1[1] = {true};
+  g.minmax(my, mx1);
+  g.sync();
   const int ak = sv.tlen - sv.plen;
-  const int ce = d.ce;
   const WfRef t = (ce == CM) ? m : ref_raw(c, s, comp_index(ce));
   const bool done = (t.lo <= ak && ak <= t.hi) && (t.at(ak) >= sv.tlen);
   if (done) { d.status = ST_END_REACHED; d.status_score = s; d.end_k = ak; return 1; }
-  if (max_ak_out) *max_ak_out = mak;
+  if (max_ak_out) *max_ak_out = my[0];
+  return 0;
+}
+
+// One score step of a direction: wavefront_compute_affine(s) followed by
+// wavefront_extend_end2end(_max)(s) and the termination check, fused into one pass over the
+// diagonals. Extending diagonal k depends only on M[k] and the sequences, and the trimmed
+// range is fixed by which M[k] are in bounds before extension, so the extended offset is
+// written once. Returns -1 on scratch overflow, 1 when the direction is finished (end
+// reached or unreachable), 0 otherwise; *max_ak receives the extension's max antidiagonal.
+template <int G>
+__device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g, int* max_ak_out) {
+  const DirCfg c = d.cfg;
+  const int nn = d.num_null, used = d.lused, nphys = d.next_phys, ce = d.ce;
+  const SeqView sv = d.sv;
+  const uint32_t tl = (uint32_t)sv.tlen, pl = (uint32_t)sv.plen;
+  *max_ak_out = 0;
+  if (c.leaf && s > c.lmax) return -1;
+  const WfRef mx = fetch(c, s - p.x, 0);
+  const WfRef mo = fetch(c, s - p.o - p.e, 0);
+  const WfRef ie = fetch(c, s - p.e, 1);
+  const WfRef de = fetch(c, s - p.e, 2);
+  const bool hx = mx.nonnull(), ho = mo.nonnull(), hie = ie.nonnull(), hde = de.nonnull();
+  if (!hx && !ho && !hie && !hde) {
+    // null step: no wavefront; the extension finds no M (wavefront_extend_end2end)
+    if (G > 1) g.sync();
+    d.num_null = nn + 1;
+    set_desc(c, s, 0, kAbsent, INT_MIN, 0, 0);
+    set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
+    set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
+    if (nn + 1 > c.scope) { d.status = ST_END_UNREACHABLE; d.status_score = s; return 1; }
+    return 0;
+  }
+  int lo = hx ? mx.lo : 1, hi = hx ? mx.hi : -1;
+  lo = min(lo, (ho ? mo.lo : 1) - 1);   hi = max(hi, (ho ? mo.hi : -1) + 1);
+  lo = min(lo, (hie ? ie.lo : 1) + 1);  hi = max(hi, (hie ? ie.hi : -1) + 1);
+  lo = min(lo, (hde ? de.lo : 1) - 1);  hi = max(hi, (hde ? de.hi : -1) - 1);
+  const bool ai = ho || hie, ad = ho || hde;
+  const int width = hi - lo + 1;
+  WfRef om, oi, od;
+  int offm = 0, offi = 0, offd = 0, need = 0;
+  if (!c.leaf) {
+    if (width > c.W) return -1;
+    om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
+    oi.base = om.base + c.W;
+    od.base = oi.base + c.W;
+    om.kbase = oi.kbase = od.kbase = 0;
+    om.mask = oi.mask = od.mask = (uint32_t)c.W - 1u;
+  } else {
+    need = width * (1 + (ai ? 1 : 0) + (ad ? 1 : 0));
+    if (used + need > d.lcap) return -1;
+    offm = used;
+    offi = offm + width;
+    offd = offi + (ai ? width : 0);
+    om.base = c.ldata + offm; oi.base = c.ldata + offi; od.base = c.ldata + offd;
+    om.kbase = oi.kbase = od.kbase = lo;
+    om.mask = oi.mask = od.mask = 0xffffffffu;
+  }
+  // r: M, I, D trimmed lo/hi, then the max antidiagonal of the extended M
+  int r[7] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN, 0};
+  for (int k = lo + g.tid; k <= hi; k += 32 * G) {
+    const int32_t ins = max(mo.get(k - 1), ie.get(k - 1)) + 1;
+    const int32_t del = max(mo.get(k + 1), de.get(k + 1));
+    const int32_t mis = mx.get(k) + 1;
+    int32_t m = max(del, max(mis, ins));
+    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
+    if (m != kNull) {
+      r[0] = min(r[0], k); r[1] = max(r[1], k);
+      m += lcp(sv, m - k, m);
+      r[6] = max(r[6], 2 * m - k);
+    }
+    om.put(k, m);
+    if (ai) {
+      oi.put(k, ins);
+      if ((uint32_t)ins <= tl && (uint32_t)(ins - k) <= pl) { r[2] = min(r[2], k); r[3] = max(r[3], k); }
+    }
+    if (ad) {
+      od.put(k, del);
+      if ((uint32_t)del <= tl && (uint32_t)(del - k) <= pl) { r[4] = min(r[4], k); r[5] = max(r[5], k); }
+    }
+  }
+  const bool mm[7] = {false, true, false, true, false, true, true};
+  g.minmax(r, mm);
+  g.sync();
+  d.num_null = 0;
+  if (c.leaf) d.lused = used + need;
+  else { c.rphys[slot_of(c, s)] = nphys; d.next_phys = (nphys + 1 == c.nphys) ? 0 : nphys + 1; }
+  if (r[0] <= r[1]) set_desc(c, s, 0, r[0], r[1], offm, lo); else set_desc(c, s, 0, lo, lo - 1, offm, lo);
+  if (ai) { if (r[2] <= r[3]) set_desc(c, s, 1, r[2], r[3], offi, lo); else set_desc(c, s, 1, lo, lo - 1, offi, lo); }
+  else set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
+  if (ad) { if (r[4] <= r[5]) set_desc(c, s, 2, r[4], r[5], offd, lo); else set_desc(c, s, 2, lo, lo - 1, offd, lo); }
+  else set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
+  // wavefront_termination_end2end on component_end at score s
+  const int ak = sv.tlen - sv.plen;
+  bool done;
+  if (ce == CM) {
+    done = (r[0] <= ak && ak <= r[1]) && (om.at(ak) >= sv.tlen);
+  } else {
+    const bool alloc = (ce == CI) ? ai : ad;
+    const WfRef& t = (ce == CI) ? oi : od;
+    const int tlo = (ce == CI) ? r[2] : r[4], thi = (ce == CI) ? r[3] : r[5];
+    done = alloc && (tlo <= ak && ak <= thi) && (t.at(ak) >= sv.tlen);
+  }
+  if (done) { d.status = ST_END_REACHED; d.status_score = s; d.end_k = ak; return 1; }
+  *max_ak_out = r[6];
   return 0;
 }
 
 struct BP { int score, sf, sr, kf, kr, of, orv, comp; };
 
 // wavefront_bialign_breakpoint_indel2indel / _m2m: the first k0 (ascending) that meets,
-// found with a ballot per 32 diagonals.
+// found with a ballot per 32 diagonals (and the lowest hitting warp for G > 1).
+template <int G>
 __device__ void bp_scan(bool is_m, bool fwd, int s0, int s1, const WfRef& w0, const WfRef& w1,
-                        int plen, int tlen, int go, int comp, BP& bp, int lane) {
+                        int plen, int tlen, int go, int comp, BP& bp, const Grp<G> g) {
   const int lo0 = w0.lo, hi0 = w0.hi;
   const int lo1 = tlen - plen - w1.hi, hi1 = tlen - plen - w1.lo;
   if (hi1 < lo0 || hi0 < lo1) return;
   const int cand = is_m ? s0 + s1 : s0 + s1 - go;
   if (!(cand < bp.score)) return;
   const int min_hi = min(hi0, hi1), max_lo = max(lo0, lo1);
-  for (int kb = max_lo; kb <= min_hi; kb += 32) {
-    const int k0 = kb + lane;
+  for (int kb = max_lo; kb <= min_hi; kb += 32 * G) {
+    const int k0 = kb + g.tid;
     bool hit = false;
     int32_t o0 = 0, o1 = 0;
     if (k0 <= min_hi) {
@@ -304,24 +463,33 @@ __device__ void bp_scan(bool is_m, bool fwd, int s0, int s1, const WfRef& w0, co
       }
     }
     const unsigned b = __ballot_sync(kFull, hit);
-    if (b) {
-      const int src = __ffs((int)b) - 1;
-      const int hk0 = __shfl_sync(kFull, k0, src);
-      const int32_t h0 = __shfl_sync(kFull, o0, src);
-      const int32_t h1 = __shfl_sync(kFull, o1, src);
-      const int hk1 = tlen - plen - hk0;
-      if (fwd) { bp.sf = s0; bp.sr = s1; bp.kf = hk0; bp.kr = hk1; bp.of = h0; bp.orv = h1; }
-      else     { bp.sf = s1; bp.sr = s0; bp.kf = hk1; bp.kr = hk0; bp.of = h1; bp.orv = h0; }
-      bp.score = cand;
-      bp.comp = comp;
-      return;
+    int src;
+    if (G == 1) {
+      if (!b) continue;
+      src = __ffs((int)b) - 1;
+    } else {
+      int first[1] = {b ? g.warp() * 32 + __ffs((int)b) - 1 : INT_MAX};
+      const bool mn[1] = {false};
+      g.minmax(first, mn);
+      if (first[0] == INT_MAX) continue;
+      src = first[0];
     }
+    const int hk0 = g.bcast(k0, src);
+    const int32_t h0 = g.bcast(o0, src);
+    const int32_t h1 = g.bcast(o1, src);
+    const int hk1 = tlen - plen - hk0;
+    if (fwd) { bp.sf = s0; bp.sr = s1; bp.kf = hk0; bp.kr = hk1; bp.of = h0; bp.orv = h1; }
+    else     { bp.sf = s1; bp.sr = s0; bp.kf = hk1; bp.kr = hk0; bp.of = h1; bp.orv = h0; }
+    bp.score = cand;
+    bp.comp = comp;
+    return;
   }
 }
 
 // wavefront_bialign_overlap (gap-affine part)
+template <int G>
 __device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s1, bool fwd, BP& bp, const Pen p,
-                                     int lane) {
+                                     const Grp<G> g) {
   const DirCfg c0 = d0.cfg, c1 = d1.cfg;
   const int plen = d0.sv.plen, tlen = d0.sv.tlen;
   const WfRef m0 = ref_raw(c0, s0, 0);
@@ -333,12 +501,12 @@ __device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s
     if (si < 0) break;
     if (s0 + si - p.o >= bp.score) continue;
     const WfRef dd1 = ref_raw(c1, si, 2);
-    if (dd0.present() && dd1.present()) bp_scan(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, lane);
+    if (dd0.present() && dd1.present()) bp_scan<G>(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, g);
     const WfRef ii1 = ref_raw(c1, si, 1);
-    if (ii0.present() && ii1.present()) bp_scan(false, fwd, s0, si, ii0, ii1, plen, tlen, p.o, CI, bp, lane);
+    if (ii0.present() && ii1.present()) bp_scan<G>(false, fwd, s0, si, ii0, ii1, plen, tlen, p.o, CI, bp, g);
     if (s0 + si >= bp.score) continue;
     const WfRef mm1 = ref_raw(c1, si, 0);
-    if (mm1.present()) bp_scan(true, fwd, s0, si, m0, mm1, plen, tlen, p.o, CM, bp, lane);
+    if (mm1.present()) bp_scan<G>(true, fwd, s0, si, m0, mm1, plen, tlen, p.o, CM, bp, g);
   }
 }
 
@@ -365,31 +533,33 @@ __device__ __forceinline__ int score_guard(const Pen& p, int plen, int tlen) {
 }
 
 // wavefront_bialign_find_breakpoint
+template <int G>
 __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, int pb, int pe, int tb, int te,
-                                            int cb, int ce, const Pen p, int max_steps, BP& bp, int lane, bool& overflow) {
+                                            int cb, int ce, const Pen p, int max_steps, BP& bp, const Grp<G> g) {
+  g.sync();
   dir_init(F, fwd_view(q, pb, pe, tb, te), cb, ce);
   dir_init(R, rev_view(q, pb, pe, tb, te), ce, cb);
-  __syncwarp();
+  g.sync();
   const int plen = pe - pb, tlen = te - tb;
   const int max_antidiag = plen + tlen - 1;
   const int guard = score_guard(p, plen, tlen);
   int sf = 0, sr = 0, fmax = 0, rmax = 0, ak = 0;
   bp.score = INT_MAX;
-  if (dir_extend(F, sf, lane, &fmax)) return F.status;
-  if (dir_extend(R, sr, lane, &rmax)) return R.status;
+  if (dir_extend<G>(F, sf, g, &fmax)) return F.status;
+  if (dir_extend<G>(R, sr, g, &rmax)) return R.status;
   bool last_fwd = false;
   for (;;) {
     if (fmax + rmax >= max_antidiag) break;
     ++sf;
-    if (!dir_compute(F, p, sf, lane)) { overflow = true; return WFG_ST_SCRATCH_OVERFLOW; }
-    const int qf = dir_extend(F, sf, lane, &ak);
+    const int qf = dir_step<G>(F, p, sf, g, &ak);
+    if (qf < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (fmax < ak) fmax = ak;
     last_fwd = true;
     if (qf) return F.status;
     if (fmax + rmax >= max_antidiag) break;
     ++sr;
-    if (!dir_compute(R, p, sr, lane)) { overflow = true; return WFG_ST_SCRATCH_OVERFLOW; }
-    const int qr = dir_extend(R, sr, lane, &ak);
+    const int qr = dir_step<G>(R, p, sr, g, &ak);
+    if (qr < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (rmax < ak) rmax = ak;
     last_fwd = false;
     if (qr) return R.status;
@@ -400,17 +570,19 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
     if (last_fwd) {
       const int min_sr = (sr > p.scope - 1) ? sr - (p.scope - 1) : 0;
       if (sf + min_sr - p.o >= bp.score) break;
-      overlap(F, R, sf, sr, true, bp, p, lane);
+      overlap<G>(F, R, sf, sr, true, bp, p, g);
       ++sr;
-      if (!dir_compute(R, p, sr, lane)) { overflow = true; return WFG_ST_SCRATCH_OVERFLOW; }
-      if (dir_extend(R, sr, lane, nullptr)) return R.status;
+      const int q = dir_step<G>(R, p, sr, g, &ak);
+      if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
+      if (q) return R.status;
     }
     const int min_sf = (sf > p.scope - 1) ? sf - (p.scope - 1) : 0;
     if (min_sf + sr - p.o >= bp.score) break;
-    overlap(R, F, sr, sf, false, bp, p, lane);
+    overlap<G>(R, F, sr, sf, false, bp, p, g);
     ++sf;
-    if (!dir_compute(F, p, sf, lane)) { overflow = true; return WFG_ST_SCRATCH_OVERFLOW; }
-    if (dir_extend(F, sf, lane, nullptr)) return F.status;
+    const int q = dir_step<G>(F, p, sf, g, &ak);
+    if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
+    if (q) return F.status;
     if (sr + sf >= max_steps) return WFG_ST_MAX_STEPS;
     if (sf > guard + 2 * p.scope || sr > guard + 2 * p.scope) return WFG_ST_UNATTAINABLE;
     last_fwd = true;
@@ -449,24 +621,31 @@ __device__ __forceinline__ long long bt_src(const DirCfg& B, int score, int ci, 
 }
 
 // Leaf: wavefront_bialign_base -> unialign -> backtrace. Appends the leaf's ops to out.
+template <int G>
 __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe, int tb, int te, int cb, int ce,
                                        const Pen p, int max_steps, RunOut& out, uint32_t* lruns, int lruns_cap,
-                          int lane, int* max_leaf_score) {
+                                       const Grp<G> g, int* max_leaf_score) {
+  g.sync();
   dir_init(B, fwd_view(q, pb, pe, tb, te), cb, ce);
-  __syncwarp();
+  g.sync();
   const int guard = score_guard(p, pe - pb, te - tb);
-  int s = 0;
-  for (;;) {
-    if (dir_extend(B, s, lane, nullptr)) break;
-    ++s;
-    if (!dir_compute(B, p, s, lane)) return WFG_ST_SCRATCH_OVERFLOW;
-    if (s >= max_steps) return WFG_ST_UNATTAINABLE;
-    if (s > guard) return WFG_ST_UNATTAINABLE;
+  int s = 0, ak = 0;
+  if (!dir_extend<G>(B, s, g, nullptr)) {
+    for (;;) {
+      ++s;
+      // wavefront_unialign_reached_limits checks the step count after compute, before extend
+      if (s >= max_steps) return WFG_ST_UNATTAINABLE;
+      if (s > guard) return WFG_ST_UNATTAINABLE;
+      const int q = dir_step<G>(B, p, s, g, &ak);
+      if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
+      if (q) break;
+    }
   }
   if (*max_leaf_score < s) *max_leaf_score = s;
   if (B.status != ST_END_REACHED) return WFG_ST_UNATTAINABLE;
   const DirCfg bc = B.cfg;
-  // Backtrace from (end_k, tlen) in component ce; runs are produced end -> begin.
+  // Backtrace from (end_k, tlen) in component ce; runs are produced end -> begin. Every
+  // thread of the group walks the same path (uniform loads, identical writes).
   const int plen = B.sv.plen, tlen = B.sv.tlen;
   int nrev = 0; int rop = -1, rlen = 0; bool rover = false;
   auto push = [&](int op, int len) {
@@ -535,7 +714,6 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
   }
   if (rlen > 0) { if (nrev < lruns_cap) lruns[nrev] = ((uint32_t)rlen << 4) | (uint32_t)rop; else rover = true; ++nrev; }
   if (rover) return WFG_ST_SCRATCH_OVERFLOW;
-  __syncwarp();
   for (int i = nrev - 1; i >= 0; --i) {
     const uint32_t r = lruns[i];
     out.emit((int)(r & 15u), (int)(r >> 4));
@@ -562,50 +740,69 @@ __device__ __forceinline__ int classic_score(int match_o, int plen, int tlen, in
 
 }  // namespace
 
-template <int WPB>
-__global__ void __launch_bounds__(WPB * 32, kMinBlocksPerSM) biwfa_persistent_kernel(KernelParams P) {
-  __shared__ Dir s_dir[WPB][3];
-  __shared__ int2 s_rdesc[WPB][2][kMaxScope * 3];
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  const long long gwarp = (long long)blockIdx.x * WPB + wib;
-  const ArenaLayout L = wfg_arena_layout(P.scope, P.ring_w, P.leaf_max_score, P.leaf_words,
+// Shared memory per group: three directions, ring descriptors and buffer map, reduction
+// scratch (dynamic shared memory holds the rings themselves when ring_in_smem).
+struct GroupSmem {
+  Dir dir[3];
+  int2 rdesc[2][kMaxScope * 3];
+  int rphys[2][kMaxScope];
+  int red[8 * 8 + 8];
+};
+
+// G warps per pair, GROUPS groups per block. RING_SMEM: the two rings of each group live
+// in dynamic shared memory (sized by the host for ring_w); otherwise in the warp arena.
+template <int G, int GROUPS, bool RING_SMEM, int MINB>
+__global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel(KernelParams P) {
+  __shared__ GroupSmem s_grp[GROUPS];
+  extern __shared__ __align__(16) int32_t s_ring_dyn[];
+  const int gib = threadIdx.x / (32 * G);
+  GroupSmem& S = s_grp[gib];
+  Grp<G> g;
+  g.tid = threadIdx.x % (32 * G);
+  g.bar = 1 + gib;
+  g.red = S.red;
+  const long long ggroup = (long long)blockIdx.x * GROUPS + gib;
+  const int nphys = P.ring_nphys > 0 ? P.ring_nphys : P.scope;
+  const ArenaLayout L = wfg_arena_layout(RING_SMEM ? 0 : nphys, P.ring_w, P.leaf_max_score, P.leaf_words,
                                          P.run_cap, P.leaf_run_cap, P.stack_cap);
-  uint8_t* arena = P.arena + gwarp * P.arena_bytes;
-  int32_t* ring = (int32_t*)(arena + L.ring_off);
+  uint8_t* arena = P.arena + ggroup * P.arena_bytes;
+  const size_t ring_dir = (size_t)nphys * 3 * P.ring_w;
+  int32_t* ring = RING_SMEM ? s_ring_dyn + (size_t)gib * 2 * ring_dir : (int32_t*)(arena + L.ring_off);
   int4* ldesc = (int4*)(arena + L.ldesc_off);
   int32_t* ldata = (int32_t*)(arena + L.ldata_off);
   uint32_t* runs = (uint32_t*)(arena + L.runs_off);
   uint32_t* lruns = (uint32_t*)(arena + L.lruns_off);
   int* stack = (int*)(arena + L.stack_off);
 
-  Dir& F = s_dir[wib][0];
-  Dir& R = s_dir[wib][1];
-  Dir& B = s_dir[wib][2];
-  const size_t ring_dir = (size_t)P.scope * 3 * P.ring_w;
+  Dir& F = S.dir[0];
+  Dir& R = S.dir[1];
+  Dir& B = S.dir[2];
   const uint32_t magic = (uint32_t)(0xffffffffu / (uint32_t)P.scope) + 1u;
   DirCfg fc{};
-  fc.leaf = 0; fc.scope = P.scope; fc.magic = magic; fc.W = P.ring_w; fc.lmax = 0;
-  fc.rdesc = s_rdesc[wib][0]; fc.rdata = ring;
+  fc.leaf = 0; fc.scope = P.scope; fc.magic = magic; fc.W = P.ring_w; fc.nphys = nphys; fc.lmax = 0;
+  fc.rdesc = S.rdesc[0]; fc.rphys = S.rphys[0]; fc.rdata = ring;
   DirCfg rc = fc;
-  rc.rdesc = s_rdesc[wib][1]; rc.rdata = ring + ring_dir;
+  rc.rdesc = S.rdesc[1]; rc.rphys = S.rphys[1]; rc.rdata = ring + ring_dir;
   DirCfg bcfg{};
-  bcfg.leaf = 1; bcfg.scope = P.scope; bcfg.magic = magic; bcfg.W = 0; bcfg.lmax = P.leaf_max_score;
+  bcfg.leaf = 1; bcfg.scope = P.scope; bcfg.magic = magic; bcfg.W = 0; bcfg.nphys = 1; bcfg.lmax = P.leaf_max_score;
   bcfg.ldesc = ldesc; bcfg.ldata = ldata;
   F.cfg = fc; R.cfg = rc; B.cfg = bcfg;
   F.lcap = R.lcap = 0; F.lused = R.lused = 0;
   B.lcap = P.leaf_words; B.lused = 0;
-  __syncwarp();
+  g.sync();
   const Pen pen = {P.x, P.o, P.e, P.scope};
 
   const unsigned long long num_pairs =
       P.num_pairs_ptr ? *P.num_pairs_ptr : (unsigned long long)P.num_pairs;
   for (;;) {
-    unsigned long long widx = 0;
-    if (lane == 0) widx = atomicAdd(P.queue_head, 1ull);
-    widx = __shfl_sync(kFull, widx, 0);
-    if (widx >= num_pairs) break;
-    const int pi = P.order[widx];
+    int widx_i = 0;
+    if (g.tid == 0) {
+      const unsigned long long w = atomicAdd(P.queue_head, 1ull);
+      widx_i = w >= num_pairs ? -1 : (int)w;
+    }
+    widx_i = g.bcast(widx_i, 0);
+    if (widx_i < 0) break;
+    const int pi = P.order[widx_i];
     const PairDesc pd = P.pairs[pi];
     PairSeqs q;
     q.pf = P.words + pd.word_off;
@@ -620,8 +817,8 @@ __global__ void __launch_bounds__(WPB * 32, kMinBlocksPerSM) biwfa_persistent_ke
 
     if (P.score_only) {
       // wavefront_bialign_compute_score (wavefront/wavefront_bialign.c:662-699)
-      BP bp; bool ovf = false;
-      const int st = find_breakpoint(F, R, q, 0, q.plen, 0, q.tlen, CM, CM, pen, P.max_steps, bp, lane, ovf);
+      BP bp;
+      const int st = find_breakpoint<G>(F, R, q, 0, q.plen, 0, q.tlen, CM, CM, pen, P.max_steps, bp, g);
       if (st == ST_OK || st == ST_END_REACHED) {
         const int wf = (st == ST_END_REACHED) ? (F.status == ST_END_REACHED ? F.status_score : R.status_score) : bp.score;
         score = classic_score(P.match_o, q.plen, q.tlen, wf);
@@ -644,26 +841,26 @@ __global__ void __launch_bounds__(WPB * 32, kMinBlocksPerSM) biwfa_persistent_ke
       push(0, q.plen, 0, q.tlen, CM, CM, min_len ? 0 : INT_MAX, 0);
       while (sp > 0 && status == ST_OK) {
         --sp;
-        __syncwarp();
         const int* e = stack + sp * 8;
         const int pb = e[0], pe = e[1], tb = e[2], te = e[3], cb = e[4], ce = e[5], rem = e[6], lvl = e[7];
-        __syncwarp();
         if (lvl > max_depth) max_depth = lvl;
         const int pl = pe - pb, tl = te - tb;
         if (tl == 0) { out.emit(WFG_OP_DEL, pl); continue; }
         if (pl == 0) { out.emit(WFG_OP_INS, tl); continue; }
         if (rem <= kFallbackMinScore) {
-          const int st = leaf_align(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns, P.leaf_run_cap, lane, &max_leaf);
+          const int st = leaf_align<G>(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns, P.leaf_run_cap, g,
+                                       &max_leaf);
           if (st != ST_OK) status = st;
           continue;
         }
-        BP bp; bool ovf = false;
-        const int st = find_breakpoint(F, R, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, bp, lane, ovf);
+        BP bp;
+        const int st = find_breakpoint<G>(F, R, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, bp, g);
         if (st != ST_OK) {
           if (st == ST_END_REACHED) {
             const int reached = (F.status == ST_END_REACHED) ? F.status_score : R.status_score;
             if (reached <= kRecoveryMinScore) {
-              const int st2 = leaf_align(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns, P.leaf_run_cap, lane, &max_leaf);
+              const int st2 = leaf_align<G>(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns,
+                                            P.leaf_run_cap, g, &max_leaf);
               if (st2 != ST_OK) status = st2;
             } else {
               status = WFG_ST_UNATTAINABLE;
@@ -680,35 +877,40 @@ __global__ void __launch_bounds__(WPB * 32, kMinBlocksPerSM) biwfa_persistent_ke
             !push(pb, pb + bv, tb, tb + bh, cb, bp.comp, bp.sf, lvl + 1)) {
           status = WFG_ST_SCRATCH_OVERFLOW;
         }
-        __syncwarp();
       }
       out.flush();
       if (status == ST_OK && out.overflow) status = WFG_ST_SCRATCH_OVERFLOW;
       if (status == ST_OK) status = WFG_ST_COMPLETED;
-      __syncwarp();
+      g.sync();
       if (status == WFG_ST_COMPLETED) {
         score = (out.n > 0) ? rescore_runs(runs, out.n, P.match_o, P.x_o, P.o_o, P.e_o) : 0;
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(P.out_head, (unsigned long long)out.n);
-        base = __shfl_sync(kFull, base, 0);
-        if ((long long)base + out.n > P.out_cap) {
+        int base_lo = 0, base_hi = 0;
+        if (g.tid == 0) {
+          const unsigned long long b = atomicAdd(P.out_head, (unsigned long long)out.n);
+          base_lo = (int)(b & 0xffffffffull);
+          base_hi = (int)(b >> 32);
+        }
+        base_lo = g.bcast(base_lo, 0);
+        base_hi = g.bcast(base_hi, 0);
+        const long long base = (long long)(((unsigned long long)(unsigned)base_hi << 32) | (unsigned)base_lo);
+        if (base + out.n > P.out_cap) {
           status = WFG_ST_OUTPUT_OVERFLOW;
         } else {
-          for (int i = lane; i < out.n; i += 32) P.out_runs[base + i] = runs[i];
-          if (lane == 0) { P.run_off[pi] = (int64_t)base; P.run_len[pi] = out.n; }
+          for (int i = g.tid; i < out.n; i += 32 * G) P.out_runs[base + i] = runs[i];
+          if (g.tid == 0) { P.run_off[pi] = (int64_t)base; P.run_len[pi] = out.n; }
         }
       }
     }
     if (status == WFG_ST_SCRATCH_OVERFLOW && P.retry_out != nullptr) {
       // Hand the pair to the next pass (larger arena); its results are written there.
-      if (lane == 0) {
+      if (g.tid == 0) {
         const unsigned long long slot = atomicAdd(P.retry_count, 1ull);
         P.retry_out[slot] = pi;
       }
-      __syncwarp();
+      g.sync();
       continue;
     }
-    if (lane == 0) {
+    if (g.tid == 0) {
       P.scores[pi] = score;
       P.status[pi] = status;
       if (status != WFG_ST_COMPLETED || P.score_only) { P.run_off[pi] = 0; P.run_len[pi] = 0; }
@@ -719,7 +921,7 @@ __global__ void __launch_bounds__(WPB * 32, kMinBlocksPerSM) biwfa_persistent_ke
         P.stats[pi * 4 + 3] = 0;
       }
     }
-    __syncwarp();
+    g.sync();
   }
 }
 
@@ -766,20 +968,50 @@ __global__ void pack_pairs_kernel(int n, const uint8_t* __restrict__ ascii, Pair
 }
 
 // ------------------------------------------------------------------ host launchers
-template <int WPB>
-static cudaError_t launch_biwfa_impl(const KernelParams& p, int grid, cudaStream_t stream) {
-  biwfa_persistent_kernel<WPB><<<grid, WPB * 32, 0, stream>>>(p);
+namespace {
+
+// Execution shapes: (warps per pair, groups per block, rings in shared memory).
+template <int G, int GROUPS, bool RS, int MINB>
+cudaError_t launch_shape(const KernelParams& p, int grid, cudaStream_t stream) {
+  const size_t dyn = RS ? (size_t)GROUPS * 2 * (size_t)(p.ring_nphys > 0 ? p.ring_nphys : p.scope) * 3 *
+                              (size_t)p.ring_w * sizeof(int32_t)
+                        : 0;
+  if (dyn > 0) {
+    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+  }
+  biwfa_persistent_kernel<G, GROUPS, RS, MINB><<<grid, G * GROUPS * 32, dyn, stream>>>(p);
   return cudaGetLastError();
 }
+
+}  // namespace
 
 int biwfa_warps_per_block() { return 4; }
 
 cudaError_t biwfa_occupancy(int* blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<4>, 4 * 32, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<1, 4, false, 6>,
+                                                       4 * 32, 0);
+}
+
+// Groups (pairs in flight) per block of a shape.
+int biwfa_groups_per_block(int group_warps, int ring_in_smem) {
+  (void)ring_in_smem;
+  return group_warps <= 1 ? 4 : 1;
 }
 
 cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream) {
-  return launch_biwfa_impl<4>(p, grid, stream);
+  const int gw = p.group_warps > 0 ? p.group_warps : 1;
+  if (gw == 1) return launch_shape<1, 4, false, 6>(p, grid, stream);
+  if (gw == 8) {
+    if (p.ring_in_smem) return launch_shape<8, 1, true, 1>(p, grid, stream);
+    return launch_shape<8, 1, false, 2>(p, grid, stream);
+  }
+  if (gw == 4) {
+    if (p.ring_in_smem) return launch_shape<4, 1, true, 1>(p, grid, stream);
+    return launch_shape<4, 1, false, 3>(p, grid, stream);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_pack(int n, const uint8_t* ascii, PairDesc* pairs, uint32_t* words, int num_sms,

@@ -78,7 +78,20 @@ struct KernelParams {
   unsigned long long* out_head;  // dense output cursor (shared by all passes)
   // statistics (optional, may be null): per pair {n_steps, max_leaf_score, max_depth, n_cells}
   int* stats;
+  // execution shape (0 = defaults): warps cooperating on one pair, rings in shared memory,
+  // physical ring buffers per direction (<= scope; see ring_buffers())
+  int group_warps;
+  int ring_in_smem;
+  int ring_nphys;
 };
+
+// Physical ring buffers a direction needs: scores that can hold a wavefront are multiples of
+// g = gcd(x, o+e, e), so any window of `scope` consecutive scores holds at most ceil(scope/g)
+// live wavefronts, and round-robin buffers of that count are never overwritten while needed.
+WFG_HD constexpr inline int wfg_gcd(int a, int b) { return b == 0 ? a : wfg_gcd(b, a % b); }
+WFG_HD constexpr inline int wfg_ring_buffers(int x, int o, int e) {
+  return ((o + e > x ? o + e : x) + 1 + wfg_gcd(wfg_gcd(x, o + e), e) - 1) / wfg_gcd(wfg_gcd(x, o + e), e);
+}
 
 // Per-warp arena carving (bytes); all offsets 256-byte aligned.
 struct ArenaLayout {

@@ -20,61 +20,12 @@
 #include <vector>
 
 #include "../../include/wfa_gpu.h"
+#include "wfg_context.h"
 #include "wfg_internal.h"
-
-namespace wfg {
-cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream);
-cudaError_t biwfa_occupancy(int* blocks_per_sm);
-int biwfa_warps_per_block();
-cudaError_t launch_pack(int n, const uint8_t* ascii, PairDesc* pairs, uint32_t* words, int num_sms,
-                        cudaStream_t stream);
-}  // namespace wfg
 
 using namespace wfg;
 
 namespace {
-
-template <typename T>
-struct DevBuf {
-  T* ptr = nullptr;
-  size_t cap = 0;  // elements
-  cudaError_t reserve(size_t n) {
-    if (n <= cap && ptr != nullptr) return cudaSuccess;
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    cap = 0;
-    size_t want = std::max<size_t>(n, 1);
-    cudaError_t e = cudaMalloc((void**)&ptr, want * sizeof(T));
-    if (e == cudaSuccess) cap = want;
-    return e;
-  }
-  void release() {
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    cap = 0;
-  }
-};
-
-template <typename T>
-struct PinBuf {
-  T* ptr = nullptr;
-  size_t cap = 0;
-  cudaError_t reserve(size_t n) {
-    if (n <= cap && ptr != nullptr) return cudaSuccess;
-    if (ptr) cudaFreeHost(ptr);
-    ptr = nullptr;
-    cap = 0;
-    size_t want = std::max<size_t>(n, 1);
-    cudaError_t e = cudaMallocHost((void**)&ptr, want * sizeof(T));
-    if (e == cudaSuccess) cap = want;
-    return e;
-  }
-  void release() {
-    if (ptr) cudaFreeHost(ptr);
-    ptr = nullptr;
-    cap = 0;
-  }
-};
 
 uint32_t next_pow2(uint64_t v) {
   uint64_t p = 1;
@@ -82,60 +33,14 @@ uint32_t next_pow2(uint64_t v) {
   return (uint32_t)std::min<uint64_t>(p, 1u << 30);
 }
 
-constexpr int kNumPasses = 3;
-constexpr int kCountersPerPass = 4;  // [queue head, retry count, -, -]
-constexpr int kOutHeadIndex = kNumPasses * kCountersPerPass;
-constexpr int kNumCounters = kOutHeadIndex + 4;
-
 }  // namespace
 
-struct wfg_context {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  // batch
-  int n = 0;
-  int64_t seq_len = 0;
-  int max_plen = 0, max_tlen = 0, max_sum = 0;
-  std::vector<int> h_plen, h_tlen;
-  std::vector<PairDesc> h_pairs;
-  std::vector<int> h_order;
-  std::vector<float> h_pred;
-  bool have_order = false, have_pred = false;
-  int64_t total_words = 0;
-  int64_t out_cap = 0;
-  DevBuf<uint8_t> d_seq;
-  DevBuf<PairDesc> d_pairs;
-  DevBuf<uint32_t> d_words;
-  DevBuf<int> d_order;
-  DevBuf<int> d_retry;  // kNumPasses-1 lists of n
-  DevBuf<int> d_scores, d_status, d_runlen;
-  DevBuf<int64_t> d_runoff;
-  DevBuf<uint32_t> d_runs;
-  DevBuf<unsigned long long> d_counters;
-  DevBuf<uint8_t> d_arena;
-  DevBuf<uint8_t> d_flush;
-  PinBuf<unsigned long long> h_counters;
-  PinBuf<PairDesc> h_pairs_pinned;
-  cudaEvent_t ev[8] = {};
-  wfg_stats_t stats{};
-  bool ran = false;
-  int last_score_only = 0;
-  int limit_ring_w = 0, limit_leaf_words = 0;
-};
-
-static int fail(wfg_context* c, cudaError_t e, const char* where) {
+int wfg_fail(wfg_context* c, cudaError_t e, const char* where) {
   if (c) {
     c->err = std::string(where) + ": " + cudaGetErrorString(e);
   }
   return WF_STATUS_DEVICE_ERROR;
 }
-#define WFG_CHECK(c, call)                                 \
-  do {                                                     \
-    cudaError_t _e = (call);                               \
-    if (_e != cudaSuccess) return fail((c), _e, #call);    \
-  } while (0)
 
 extern "C" {
 
@@ -146,7 +51,8 @@ wfg_context_t* wfg_context_create(int device) {
   wfg_context* c = new wfg_context();
   c->device = device;
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return nullptr;
   }
@@ -168,6 +74,7 @@ void wfg_context_destroy(wfg_context_t* c) {
   c->d_flush.release(); c->h_counters.release(); c->h_pairs_pinned.release();
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
+  cudaStreamDestroy(c->aux_stream);
   delete c;
 }
 
@@ -182,6 +89,7 @@ int wfg_upload(wfg_context_t* c, int n, const char* seq, int64_t seq_len, const 
   c->h_plen.assign(plen, plen + n);
   c->h_tlen.assign(tlen, tlen + n);
   c->have_order = c->have_pred = false;
+  c->feats_valid = c->pred_valid = false;
   c->max_plen = c->max_tlen = c->max_sum = 0;
   int64_t words = 0, out_cap = 0;
   WFG_CHECK(c, cudaStreamSynchronize(c->stream));  // host staging buffers are reused below
@@ -255,14 +163,8 @@ int wfg_set_predictions(wfg_context_t* c, const float* pred) {
 
 namespace {
 
-struct PassShape {
-  int ring_w, leaf_words, leaf_max_score, run_cap, leaf_run_cap, stack_cap;
-  int64_t warps;
-  ArenaLayout L;
-};
-
 // Internal penalties (WFA2-lib wavefront_penalties_set_affine, wavefront_penalties.c:95-130).
-struct IntPen { int x, o, e, scope; };
+struct IntPen { int x, o, e, scope, nphys; };
 IntPen internal_penalties(const wfg_config_t* cfg) {
   IntPen p;
   if (cfg->match < 0) {
@@ -273,6 +175,7 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
     p.x = cfg->mismatch; p.o = cfg->gap_opening; p.e = cfg->gap_extension;
   }
   p.scope = std::max(p.o + p.e, p.x) + 1;
+  p.nphys = wfg_ring_buffers(p.x, p.o, p.e);
   return p;
 }
 
@@ -283,9 +186,20 @@ int leaf_score_bound(const IntPen& p) {
   return std::max(520, short_pair) + 8;
 }
 
-PassShape shape_pass(const wfg_context* c, const IntPen& p, int pass, int ring_w_hint) {
-  if (pass == 0 && c->limit_ring_w > 0) ring_w_hint = c->limit_ring_w;
-  PassShape s;
+// One persistent launch: execution shape, arena carving and the pairs it drains.
+struct Launch {
+  int gw = 1;            // warps per pair
+  int smem = 0;          // rings in shared memory
+  int ring_w = 0, leaf_words = 0, leaf_max_score = 0, run_cap = 0, leaf_run_cap = 0, stack_cap = 0;
+  int64_t groups = 0;    // pairs in flight
+  ArenaLayout L{};
+  int64_t arena_off = 0; // byte offset of this launch's arenas
+  int order_off = 0, count = 0;
+};
+
+// Scratch sizes of a pass: pass 0 is bounded by the ring hint (predicted width or the plain
+// cap) and a small leaf store; the retry passes size rings from the longest pair.
+void size_launch(const wfg_context* c, const IntPen& p, int pass, int ring_w_hint, Launch& s) {
   const int maxsum = std::max(c->max_sum, 1);
   const uint32_t ring_full = next_pow2((uint64_t)maxsum + 8);
   s.leaf_max_score = leaf_score_bound(p);
@@ -299,7 +213,8 @@ PassShape shape_pass(const wfg_context* c, const IntPen& p, int pass, int ring_w
     leaf_full += 3LL * std::min<int64_t>(maxsum + 8, 2LL * sc / std::max(p.e, 1) + 8);
   leaf_full = std::min<int64_t>(leaf_full, (int64_t)1 << 28);
   if (pass == 0) {
-    s.ring_w = ring_w_hint > 0 ? (int)std::min<uint32_t>(next_pow2((uint64_t)ring_w_hint), ring_full) : (int)ring_full;
+    const uint32_t plain_cap = std::min<uint32_t>(ring_full, kPlainRingCap);
+    s.ring_w = ring_w_hint > 0 ? (int)std::min<uint32_t>(next_pow2((uint64_t)ring_w_hint), ring_full) : (int)plain_cap;
     s.leaf_words = (int)std::min<int64_t>(leaf_full, 1 << 16);
     if (c->limit_leaf_words > 0) s.leaf_words = std::max(c->limit_leaf_words, 16);
   } else if (pass == 1) {
@@ -310,9 +225,26 @@ PassShape shape_pass(const wfg_context* c, const IntPen& p, int pass, int ring_w
     s.leaf_words = (int)leaf_full;
     s.stack_cap = 256;
   }
-  s.L = wfg_arena_layout(p.scope, s.ring_w, s.leaf_max_score, s.leaf_words, s.run_cap, s.leaf_run_cap, s.stack_cap);
-  s.warps = 0;
-  return s;
+  if (s.smem) {
+    // Both rings of the group in dynamic shared memory: the widest power of two that keeps
+    // them within kSmemRingBytes; penalties with many live buffers fall back to HBM rings.
+    int w = kSmemRingW;
+    while (w >= 64 && (int64_t)2 * p.nphys * 3 * w * 4 > kSmemRingBytes) w >>= 1;
+    if (w < 64) s.smem = 0;
+    else s.ring_w = std::min(s.ring_w, w);
+  }
+  s.L = wfg_arena_layout(s.smem ? 0 : p.nphys, s.ring_w, s.leaf_max_score, s.leaf_words, s.run_cap, s.leaf_run_cap,
+                         s.stack_cap);
+}
+
+// Groups that fit the device at once for a shape (persistent grid).
+int64_t max_groups(const wfg_context* c, int gw) {
+  if (gw <= 1) {
+    int bps = 0;
+    if (biwfa_occupancy(&bps) != cudaSuccess || bps < 1) bps = 1;
+    return (int64_t)bps * c->num_sms * biwfa_groups_per_block(1, 0);
+  }
+  return (int64_t)c->num_sms * (gw == 4 ? 2 : 1);
 }
 
 }  // namespace
@@ -330,30 +262,69 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     c->err = "max_score_scope above 32 is not supported";
     return WF_STATUS_UNSUPPORTED;
   }
+  if ((int64_t)(c->max_sum + 16) * (int64_t)std::max(p.x, p.o + p.e) >= ((int64_t)1 << 26)) {
+    c->err = "pair too long for 27-bit scores";
+    return WF_STATUS_UNSUPPORTED;
+  }
   cudaSetDevice(c->device);
   const int n = c->n;
   const int64_t h2d_upload = c->stats.h2d_bytes;
   c->stats = wfg_stats_t{};
   c->stats.h2d_bytes = h2d_upload + (int64_t)sizeof(int) * n;  // upload + processing order
   c->last_score_only = cfg->score_only;
-  // ---- order
+  // ---- order and pass-0 launches
   std::vector<int> order((size_t)n);
-  int ring_hint = 0;
+  std::vector<Launch> first;  // concurrent pass-0 launches
   if (sched == WFG_SCHED_GIVEN && c->have_order) {
     order = c->h_order;
-  } else if (sched == WFG_SCHED_LEARNED && c->have_pred) {
-    // Longest predicted work first; the ring is sized for the largest predicted score
-    // (with margin); mispredicted pairs overflow into the next pass.
-    std::iota(order.begin(), order.end(), 0);
-    std::vector<double> cost((size_t)n);
-    float maxpred = 0.f;
-    for (int i = 0; i < n; ++i) {
-      const double s = std::max(1.0f, c->h_pred[(size_t)i]);
-      cost[(size_t)i] = s * s + (double)(c->h_plen[(size_t)i] + c->h_tlen[(size_t)i]);
-      maxpred = std::max(maxpred, c->h_pred[(size_t)i]);
+    Launch l; l.gw = c->force_gw; l.smem = c->force_smem; l.count = n;
+    first.push_back(l);
+  } else if (sched == WFG_SCHED_LEARNED && (c->have_pred || c->model != nullptr)) {
+    if (c->model != nullptr) {
+      // Predict on the device (4-mer features + MLP), then bin on the host.
+      const int st = wfg_model_predict(c->model, c, nullptr);
+      if (st != WF_STATUS_ALG_COMPLETED) return st;
+      c->h_pred.resize((size_t)n);
+      if (n > 0) {
+        WFG_CHECK(c, cudaMemcpyAsync(c->h_pred.data(), c->d_pred.ptr, sizeof(float) * (size_t)n,
+                                     cudaMemcpyDeviceToHost, c->stream));
+        WFG_CHECK(c, cudaStreamSynchronize(c->stream));
+      }
     }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[(size_t)a] > cost[(size_t)b]; });
-    ring_hint = (int)(2.0 * (1.25 * maxpred + 64) / std::max(p.e, 1) + 16);
+    // Wide pairs (predicted score above the threshold) go to a multi-warp launch on a second
+    // stream, the rest to the single-warp launch; each group is ordered by predicted work,
+    // largest first, and its rings are sized from its largest prediction (a mispredicted
+    // pair overflows into the retry passes).
+    const float thr = c->tune.wide_threshold;
+    std::vector<int> wide, narrow;
+    float max_wide = 0.f, max_narrow = 0.f;
+    for (int i = 0; i < n; ++i) {
+      const float s = c->h_pred[(size_t)i];
+      if (c->tune.wide_warps > 1 && s >= thr) { wide.push_back(i); max_wide = std::max(max_wide, s); }
+      else { narrow.push_back(i); max_narrow = std::max(max_narrow, s); }
+    }
+    auto by_pred = [&](int a, int b) {
+      const float pa = c->h_pred[(size_t)a], pb = c->h_pred[(size_t)b];
+      if (pa != pb) return pa > pb;
+      return c->h_plen[(size_t)a] + c->h_tlen[(size_t)a] > c->h_plen[(size_t)b] + c->h_tlen[(size_t)b];
+    };
+    std::stable_sort(wide.begin(), wide.end(), by_pred);
+    std::stable_sort(narrow.begin(), narrow.end(), by_pred);
+    std::copy(wide.begin(), wide.end(), order.begin());
+    std::copy(narrow.begin(), narrow.end(), order.begin() + (ptrdiff_t)wide.size());
+    const double m = c->tune.ring_margin;
+    if (!wide.empty()) {
+      Launch l; l.gw = c->tune.wide_warps; l.order_off = 0; l.count = (int)wide.size();
+      const int w_need = (int)(m * max_wide / std::max(p.e, 1)) + 64;
+      l.smem = (c->tune.wide_smem && next_pow2((uint64_t)w_need) <= (uint32_t)kSmemRingW) ? 1 : 0;
+      l.ring_w = w_need;
+      first.push_back(l);
+    }
+    if (!narrow.empty()) {
+      Launch l; l.gw = 1; l.order_off = (int)wide.size(); l.count = (int)narrow.size();
+      l.ring_w = (int)(m * max_narrow / std::max(p.e, 1)) + 64;
+      first.push_back(l);
+    }
   } else {
     // Plain path: longest pairs first, a stable counting sort on plen + tlen (O(n)).
     std::vector<int> cnt((size_t)c->max_sum + 2, 0);
@@ -361,25 +332,37 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     for (size_t v = 1; v < cnt.size(); ++v) cnt[v] += cnt[v - 1];
     for (int i = 0; i < n; ++i)
       order[(size_t)cnt[(size_t)(c->max_sum - (c->h_plen[(size_t)i] + c->h_tlen[(size_t)i]))]++] = i;
+    Launch l; l.gw = c->force_gw; l.smem = c->force_smem; l.count = n;
+    first.push_back(l);
   }
-  // ---- pass shapes and arena
-  int bps = 0;
-  WFG_CHECK(c, biwfa_occupancy(&bps));
-  const int wpb = biwfa_warps_per_block();
-  const int64_t max_warps = (int64_t)std::max(bps, 1) * c->num_sms * wpb;
-  const int64_t arena_budget = (int64_t)24 << 30;  // bytes of HBM for per-warp arenas
-  PassShape shapes[kNumPasses];
-  int64_t arena_need = 0;
-  for (int ps = 0; ps < kNumPasses; ++ps) {
-    shapes[ps] = shape_pass(c, p, ps, ring_hint);
-    int64_t w = std::min<int64_t>(max_warps, std::max<int64_t>(wpb, (int64_t)n));
-    if (ps == 1) w = std::min<int64_t>(w, (int64_t)c->num_sms * wpb * 2);
-    if (ps == 2) w = std::min<int64_t>(w, (int64_t)c->num_sms * wpb);
-    const int64_t fit = arena_budget / std::max<int64_t>(shapes[ps].L.total, 1);
-    w = std::max<int64_t>(wpb, std::min<int64_t>(w, fit));
-    w = (w / wpb) * wpb;
-    shapes[ps].warps = w;
-    arena_need = std::max(arena_need, w * shapes[ps].L.total);
+  if (first.empty()) { Launch l; l.count = 0; first.push_back(l); }
+  // ---- shapes and arena (pass-0 launches run concurrently; retry passes reuse the arena)
+  const int64_t arena_budget = (int64_t)24 << 30;
+  int64_t pass0_bytes = 0;
+  for (Launch& l : first) {
+    if (l.gw < 1) l.gw = 1;
+    if (l.gw != 1 && l.gw != 4 && l.gw != 8) l.gw = 8;
+    const int hint = l.ring_w > 0 ? l.ring_w : c->limit_ring_w;
+    size_launch(c, p, 0, hint, l);
+    int64_t gmax = std::min<int64_t>(max_groups(c, l.gw), std::max<int64_t>(1, l.count));
+    const int64_t fit = (arena_budget / (int64_t)first.size()) / std::max<int64_t>(l.L.total, 1);
+    l.groups = std::max<int64_t>(1, std::min(gmax, fit));
+    const int gpb = biwfa_groups_per_block(l.gw, l.smem);
+    l.groups = std::max<int64_t>(gpb, (l.groups / gpb) * gpb);
+    l.arena_off = pass0_bytes;
+    pass0_bytes += l.groups * l.L.total;
+  }
+  Launch retry[kNumPasses];
+  int64_t arena_need = pass0_bytes;
+  for (int ps = 1; ps < kNumPasses; ++ps) {
+    Launch& l = retry[ps];
+    l.gw = 1;
+    size_launch(c, p, ps, 0, l);
+    int64_t gmax = std::min<int64_t>(max_groups(c, 1), std::max<int64_t>(4, (int64_t)n));
+    gmax = std::min<int64_t>(gmax, ps == 1 ? (int64_t)c->num_sms * 4 : (int64_t)c->num_sms * 2);
+    const int64_t fit = arena_budget / std::max<int64_t>(l.L.total, 1);
+    l.groups = std::max<int64_t>(4, (std::min(gmax, fit) / 4) * 4);
+    arena_need = std::max(arena_need, l.groups * l.L.total);
   }
   WFG_CHECK(c, c->d_arena.reserve((size_t)arena_need));
   if (n > 0) WFG_CHECK(c, cudaMemcpyAsync(c->d_order.ptr, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
@@ -387,30 +370,22 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   WFG_CHECK(c, cudaMemsetAsync(c->d_counters.ptr, 0, sizeof(unsigned long long) * kNumCounters, c->stream));
   WFG_CHECK(c, launch_pack(n, c->d_seq.ptr, c->d_pairs.ptr, c->d_words.ptr, c->num_sms, c->stream));
   WFG_CHECK(c, cudaEventRecord(c->ev[1], c->stream));
-  int launches = 1;
-  for (int ps = 0; ps < kNumPasses; ++ps) {
-    const PassShape& s = shapes[ps];
+  auto params = [&](const Launch& l, int ps) {
     KernelParams kp{};
     kp.x = p.x; kp.o = p.o; kp.e = p.e; kp.scope = p.scope;
     kp.match_o = cfg->match; kp.x_o = cfg->mismatch; kp.o_o = cfg->gap_opening; kp.e_o = cfg->gap_extension;
     kp.score_only = cfg->score_only;
     kp.max_steps = cfg->max_alignment_steps > 0 ? cfg->max_alignment_steps : INT_MAX;
-    kp.num_pairs = n;
-    kp.num_pairs_ptr = (ps == 0) ? nullptr : c->d_counters.ptr + (ps - 1) * kCountersPerPass + 1;
     kp.pairs = c->d_pairs.ptr;
-    kp.order = (ps == 0) ? c->d_order.ptr : c->d_retry.ptr + (size_t)(ps - 1) * n;
-    kp.retry_out = (ps + 1 < kNumPasses) ? c->d_retry.ptr + (size_t)ps * n : nullptr;
-    kp.retry_count = c->d_counters.ptr + ps * kCountersPerPass + 1;
-    kp.queue_head = c->d_counters.ptr + ps * kCountersPerPass + 0;
     kp.words = c->d_words.ptr;
-    kp.arena = c->d_arena.ptr;
-    kp.arena_bytes = s.L.total;
-    kp.ring_w = s.ring_w;
-    kp.leaf_words = s.leaf_words;
-    kp.leaf_max_score = s.leaf_max_score;
-    kp.run_cap = s.run_cap;
-    kp.leaf_run_cap = s.leaf_run_cap;
-    kp.stack_cap = s.stack_cap;
+    kp.arena = c->d_arena.ptr + l.arena_off;
+    kp.arena_bytes = l.L.total;
+    kp.ring_w = l.ring_w;
+    kp.leaf_words = l.leaf_words;
+    kp.leaf_max_score = l.leaf_max_score;
+    kp.run_cap = l.run_cap;
+    kp.leaf_run_cap = l.leaf_run_cap;
+    kp.stack_cap = l.stack_cap;
     kp.scores = c->d_scores.ptr;
     kp.status = c->d_status.ptr;
     kp.run_off = c->d_runoff.ptr;
@@ -419,20 +394,74 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     kp.out_cap = c->out_cap;
     kp.out_head = c->d_counters.ptr + kOutHeadIndex;
     kp.stats = nullptr;
-    if (n > 0) {
-      WFG_CHECK(c, launch_biwfa(kp, (int)(s.warps / wpb), c->stream));
+    kp.group_warps = l.gw;
+    kp.ring_in_smem = l.smem;
+    kp.ring_nphys = p.nphys;
+    kp.retry_out = (ps + 1 < kNumPasses) ? c->d_retry.ptr + (size_t)ps * n : nullptr;
+    kp.retry_count = c->d_counters.ptr + ps * kCountersPerPass + 1;
+    return kp;
+  };
+  int launches = 1;
+  // pass 0: the first launch on the context's stream, a second one (wide pairs) on the aux
+  // stream, joined before the retry passes
+  for (size_t li = 0; li < first.size(); ++li) {
+    const Launch& l = first[li];
+    KernelParams kp = params(l, 0);
+    kp.num_pairs = l.count;
+    kp.num_pairs_ptr = nullptr;
+    kp.order = c->d_order.ptr + l.order_off;
+    kp.queue_head = c->d_counters.ptr + (li == 0 ? 0 : 2);
+    cudaStream_t st = c->stream;
+    if (li > 0) {
+      WFG_CHECK(c, cudaStreamWaitEvent(c->aux_stream, c->ev[1], 0));
+      st = c->aux_stream;
+    }
+    if (l.count > 0) {
+      WFG_CHECK(c, launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), st));
       ++launches;
     }
-    if (ps == 0) WFG_CHECK(c, cudaEventRecord(c->ev[2], c->stream));
+    if (li > 0) {
+      WFG_CHECK(c, cudaEventRecord(c->ev[4], c->aux_stream));
+      WFG_CHECK(c, cudaStreamWaitEvent(c->stream, c->ev[4], 0));
+    }
+  }
+  WFG_CHECK(c, cudaEventRecord(c->ev[2], c->stream));
+  for (int ps = 1; ps < kNumPasses; ++ps) {
+    const Launch& l = retry[ps];
+    KernelParams kp = params(l, ps);
+    kp.num_pairs = n;
+    kp.num_pairs_ptr = c->d_counters.ptr + (ps - 1) * kCountersPerPass + 1;
+    kp.order = c->d_retry.ptr + (size_t)(ps - 1) * n;
+    kp.queue_head = c->d_counters.ptr + ps * kCountersPerPass + 0;
+    if (n > 0) {
+      WFG_CHECK(c, launch_biwfa(kp, (int)(l.groups / 4), c->stream));
+      ++launches;
+    }
   }
   WFG_CHECK(c, cudaEventRecord(c->ev[3], c->stream));
   WFG_CHECK(c, cudaMemcpyAsync(c->h_counters.ptr, c->d_counters.ptr, sizeof(unsigned long long) * kNumCounters,
                                cudaMemcpyDeviceToHost, c->stream));
   c->stats.launches = launches;
-  c->stats.num_warps = (int)shapes[0].warps;
-  c->stats.ring_w = shapes[0].ring_w;
-  c->stats.arena_bytes = shapes[0].L.total;
+  c->stats.num_warps = (int)(first[0].groups * first[0].gw);
+  c->stats.ring_w = first[0].ring_w;
+  c->stats.arena_bytes = first[0].L.total;
   c->ran = true;
+  return WF_STATUS_ALG_COMPLETED;
+}
+
+int wfg_set_exec_shape(wfg_context_t* c, int group_warps, int ring_in_smem) {
+  if (!c || (group_warps != 1 && group_warps != 4 && group_warps != 8)) return WF_STATUS_UNSUPPORTED;
+  c->force_gw = group_warps;
+  c->force_smem = (group_warps > 1 && ring_in_smem) ? 1 : 0;
+  return WF_STATUS_ALG_COMPLETED;
+}
+
+int wfg_set_learned_policy(wfg_context_t* c, float wide_threshold, int wide_warps, int wide_smem, float ring_margin) {
+  if (!c || (wide_warps != 1 && wide_warps != 4 && wide_warps != 8) || ring_margin < 1.0f) return WF_STATUS_UNSUPPORTED;
+  c->tune.wide_threshold = wide_threshold;
+  c->tune.wide_warps = wide_warps;
+  c->tune.wide_smem = wide_smem ? 1 : 0;
+  c->tune.ring_margin = ring_margin;
   return WF_STATUS_ALG_COMPLETED;
 }
 

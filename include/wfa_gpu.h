@@ -270,6 +270,23 @@ int wfg_get_stats(wfg_context_t* ctx, wfg_stats_t* stats);
  * leaf store in int32 words. Pairs that do not fit overflow into the retry passes, whose
  * arenas are sized from the batch's longest pair; results never change. */
 int wfg_set_arena_limits(wfg_context_t* ctx, int ring_w, int leaf_words);
+/* Execution shape of the first pass for WFG_SCHED_PLAIN / WFG_SCHED_GIVEN: group_warps
+ * warps cooperate on one pair (1, 4 or 8); ring_in_smem keeps the wavefront rings in
+ * shared memory (group_warps > 1; rings of 1024 diagonals, wider pairs overflow into the
+ * retry passes). Results never depend on the shape. Default 1, 0. */
+int wfg_set_exec_shape(wfg_context_t* ctx, int group_warps, int ring_in_smem);
+/* Policy of WFG_SCHED_LEARNED: pairs whose predicted score is at least wide_threshold run
+ * with wide_warps warps per pair (rings in shared memory when wide_smem and they fit),
+ * concurrently with the single-warp launch for the rest; ring widths are
+ * ring_margin * predicted score / gap_extension + 64 diagonals. */
+int wfg_set_learned_policy(wfg_context_t* ctx, float wide_threshold, int wide_warps, int wide_smem,
+                           float ring_margin);
+/* Autotuner for WFG_SCHED_LEARNED (requires an attached model): runs the resident batch
+ * with each candidate policy (wide threshold x warps per pair x shared-memory rings, plus
+ * "no wide launch"), times the device work with CUDA events, keeps the fastest policy on
+ * the context and returns its time (ms) and choice. Results never depend on the policy. */
+int wfg_autotune_learned_policy(wfg_context_t* ctx, const wfg_config_t* cfg, float* best_ms,
+                                float* best_threshold, int* best_warps, int* best_smem);
 /* Write ~bytes of scratch to evict the L2 (between timed runs). */
 int wfg_flush_l2(wfg_context_t* ctx, int64_t bytes);
 /* Synchronize the context's stream. */
@@ -278,6 +295,41 @@ int wfg_synchronize(wfg_context_t* ctx);
  * speed). NULL on failure. */
 void* wfg_host_alloc(int64_t bytes);
 void wfg_host_free(void* ptr);
+
+/* ------------------------------------------------------------------ learned scheduling */
+/* No WFA2-lib counterpart. A small MLP (32 sketch features -> 64 -> 64 -> 1, ReLU, bf16
+ * weights, fp32 accumulation) predicts each pair's alignment score from its lengths and
+ * 4-mer count differences. WFG_SCHED_LEARNED runs it on the device inside wfg_run to order
+ * and bin pairs and size the first pass's scratch; a mispredicted pair overflows into a
+ * larger pass, so results never depend on the model. Training runs on the GPU with the
+ * library's own forward/backward kernels. */
+typedef struct wfg_model wfg_model_t;
+#define WFG_MODEL_FEATURES 32
+/* Number of fp32 parameters (W1 32x64, b1, W2 64x64, b2, w3, b3). */
+int wfg_model_param_count(void);
+/* A model on ctx's device, initialised from seed (He-uniform weights, zero biases). */
+wfg_model_t* wfg_model_create(wfg_context_t* ctx, uint64_t seed);
+void wfg_model_destroy(wfg_model_t* model);
+int wfg_model_get_params(wfg_model_t* model, float* params);
+int wfg_model_set_params(wfg_model_t* model, const float* params);
+/* Features of the resident batch (device); optionally copied to host as bf16 bit patterns
+ * (num_pairs x 32 uint16). */
+int wfg_features(wfg_context_t* ctx, uint16_t* host_features);
+/* Train on the resident batch: targets are alignment scores (host, num_pairs; the model
+ * regresses log(1 + |score|)). Minibatches of batch_rows, Adam with learning rate lr,
+ * rows shuffled per epoch from seed. epoch_loss (nullable, epochs entries) receives the
+ * mean squared error of each epoch. */
+int wfg_model_train(wfg_model_t* model, wfg_context_t* ctx, const int* target_scores, int epochs,
+                    int batch_rows, float lr, uint64_t seed, float* epoch_loss);
+/* Gradient of the mean squared error over all resident pairs for log-targets (host,
+ * num_pairs) at the current parameters (for checks against a float64 oracle). */
+int wfg_model_gradient(wfg_model_t* model, wfg_context_t* ctx, const float* log_targets,
+                       float* grad, float* loss);
+/* Predicted scores of the resident batch (kept on the device for WFG_SCHED_LEARNED;
+ * optionally copied to host_pred). */
+int wfg_model_predict(wfg_model_t* model, wfg_context_t* ctx, float* host_pred);
+/* Attach a model to a context: WFG_SCHED_LEARNED then predicts on the device in wfg_run. */
+int wfg_set_model(wfg_context_t* ctx, wfg_model_t* model);
 
 /* Aligning without allocating (no WFA2-lib counterpart; there is no reference interface
  * this replaces). For callers that may not allocate device memory themselves or let a
