@@ -101,7 +101,7 @@ class Stats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("pack_ms", C.c_double), ("total_ms", C.c_double),
                 ("launches", C.c_int), ("retried_pairs", C.c_int), ("num_warps", C.c_int), ("ring_w", C.c_int),
                 ("arena_bytes", C.c_int64), ("total_runs", C.c_int64), ("h2d_bytes", C.c_int64),
-                ("d2h_bytes", C.c_int64)]
+                ("d2h_bytes", C.c_int64), ("used_graph", C.c_int)]
 
 
 P = C.POINTER
@@ -137,6 +137,7 @@ SIGNATURES = {
     "wfg_get_stats": (C.c_int, [C.c_void_p, P(Stats)]),
     "wfg_set_arena_limits": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "wfg_set_exec_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "wfg_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "wfg_set_learned_policy": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_float]),
     "wfg_autotune_learned_policy": (C.c_int, [C.c_void_p, P(Config), P(C.c_float), P(C.c_float), _ip, _ip]),
     "wfg_flush_l2": (C.c_int, [C.c_void_p, C.c_int64]),

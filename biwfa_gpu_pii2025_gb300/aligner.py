@@ -179,6 +179,10 @@ class BatchAligner:
         self._check(self.lib.wfg_set_exec_shape(self.ctx, group_warps, 1 if ring_in_smem else 0),
                     "wfg_set_exec_shape")
 
+    def set_graph(self, enable: bool = True):
+        """Run each wfg_run's device work as one CUDA graph (default) or as direct launches."""
+        self._check(self.lib.wfg_set_graph(self.ctx, 1 if enable else 0), "wfg_set_graph")
+
     def set_learned_policy(self, wide_threshold=1200.0, wide_warps=8, wide_smem=True, ring_margin=1.4):
         self._check(self.lib.wfg_set_learned_policy(self.ctx, wide_threshold, wide_warps, 1 if wide_smem else 0,
                                                     ring_margin), "wfg_set_learned_policy")

@@ -18,6 +18,7 @@ CSRC = PKG / "csrc"
 ROOT = PKG.parent
 BUILD = ROOT / "_build" / "biwfa_gb300"
 LIB = PKG / "libbiwfa_gb300.so"
+CLI = PKG / "align_benchmark"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
@@ -47,19 +48,36 @@ def _compile(src: str) -> Path:
     return out
 
 
+def _build_cli() -> Path:
+    """The align_benchmark-compatible CLI (csrc/align_benchmark.cpp), linked to the library."""
+    src = CSRC / "align_benchmark.cpp"
+    deps = [src, LIB, ROOT / "include" / "wfa_gpu.h"]
+    if CLI.exists() and all(CLI.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return CLI
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("no C++ compiler for the align_benchmark CLI")
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", str(ROOT / "include"), str(src), f"-L{PKG}", "-lbiwfa_gb300",
+           "-Wl,-rpath,$ORIGIN", "-o", str(CLI)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"align_benchmark build failed:\n{res.stdout}\n{res.stderr}")
+    return CLI
+
+
 def build(verbose: bool = False) -> Path:
     BUILD.mkdir(parents=True, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
-    if LIB.exists() and all(LIB.stat().st_mtime >= o.stat().st_mtime for o in objs):
-        return LIB
-    cmd = [nvcc_path(), *ARCH, "-shared", "-cudart", "static", "-o", str(LIB), *map(str, objs),
-           "-Xlinker", "--no-undefined", "-lpthread", "-ldl", "-lrt"]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    if not (LIB.exists() and all(LIB.stat().st_mtime >= o.stat().st_mtime for o in objs)):
+        cmd = [nvcc_path(), *ARCH, "-shared", "-cudart", "static", "-o", str(LIB), *map(str, objs),
+               "-Xlinker", "--no-undefined", "-lpthread", "-ldl", "-lrt"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    _build_cli()
     if verbose:
-        print(f"built {LIB}")
+        print(f"built {LIB} and {CLI}")
     return LIB
 
 

@@ -27,7 +27,14 @@ constexpr int32_t kNull = INT32_MIN / 2;   // WAVEFRONT_OFFSET_NULL
 constexpr int kAbsent = INT32_MAX;         // lo of a wavefront that does not exist
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxScope = 32;
-constexpr int kMinBlocksPerSM = 6;  // caps registers so 24 warps fit on an SM
+#ifndef WFG_G1_MIN_BLOCKS
+#define WFG_G1_MIN_BLOCKS 6
+#endif
+#ifndef WFG_STEP_UNROLL
+#define WFG_STEP_UNROLL 2
+#endif
+constexpr int kMinBlocksPerSM = WFG_G1_MIN_BLOCKS;  // 6: caps registers so 24 warps fit on an SM
+constexpr int kStepUnroll = WFG_STEP_UNROLL;        // diagonals per thread per step iteration
 constexpr int ST_OK = -1, ST_END_REACHED = -2, ST_END_UNREACHABLE = -3;
 constexpr int CM = 0, CI = 1, CD = 3;      // components (affine2p_matrix_type values)
 constexpr int kFallbackMinScore = 250, kFallbackMinLength = 100, kRecoveryMinScore = 500;
@@ -88,6 +95,28 @@ __device__ __forceinline__ int lcp(const SeqView& s, int v, int h) {
     if (x) { n += (__ffs((int)x) - 1) >> s.bshift; break; }
     n += cpw;
     if (n >= maxn) break;
+  }
+  return min(n, maxn);
+}
+
+// lcp() split in two so that the first windows of several diagonals load together:
+// lcp_first() is the XOR of the first windows (0 when nothing can match), lcp_rest()
+// continues from it.
+__device__ __forceinline__ uint32_t lcp_first(const SeqView& s, int v, int h) {
+  if (min(s.plen - v, s.tlen - h) <= 0) return 0u;
+  return win32(s.pw, s.p0 + v, s.bshift) ^ win32(s.tw, s.t0 + h, s.bshift);
+}
+
+__device__ __forceinline__ int lcp_rest(const SeqView& s, int v, int h, uint32_t x) {
+  const int maxn = min(s.plen - v, s.tlen - h);
+  if (maxn <= 0) return 0;
+  const int cpw = 32 >> s.bshift;
+  int n = 0;
+  for (;;) {
+    if (x) { n += (__ffs((int)x) - 1) >> s.bshift; break; }
+    n += cpw;
+    if (n >= maxn) break;
+    x = win32(s.pw, s.p0 + v + n, s.bshift) ^ win32(s.tw, s.t0 + h + n, s.bshift);
   }
   return min(n, maxn);
 }
@@ -218,87 +247,6 @@ __device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
   }
 }
 
-// wavefront_compute_affine. Returns false when the scratch is too small (the pair is
-// retried with a larger arena).
-template <int G>
-__device__ __noinline__ bool dir_compute(Dir& d, const Pen p, int s, const Grp<G> g) {
-  const DirCfg c = d.cfg;
-  const int nn = d.num_null, used = d.lused, nphys = d.next_phys;
-  const uint32_t tl = (uint32_t)d.sv.tlen, pl = (uint32_t)d.sv.plen;
-  if (c.leaf && s > c.lmax) return false;
-  const WfRef mx = fetch(c, s - p.x, 0);
-  const WfRef mo = fetch(c, s - p.o - p.e, 0);
-  const WfRef ie = fetch(c, s - p.e, 1);
-  const WfRef de = fetch(c, s - p.e, 2);
-  const bool hx = mx.nonnull(), ho = mo.nonnull(), hie = ie.nonnull(), hde = de.nonnull();
-  if (!hx && !ho && !hie && !hde) {
-    if (G > 1) g.sync();
-    d.num_null = nn + 1;
-    set_desc(c, s, 0, kAbsent, INT_MIN, 0, 0);
-    set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
-    set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
-    return true;
-  }
-  // A missing input is the shared null wavefront (lo = 1, hi = -1).
-  int lo = hx ? mx.lo : 1, hi = hx ? mx.hi : -1;
-  lo = min(lo, (ho ? mo.lo : 1) - 1);   hi = max(hi, (ho ? mo.hi : -1) + 1);
-  lo = min(lo, (hie ? ie.lo : 1) + 1);  hi = max(hi, (hie ? ie.hi : -1) + 1);
-  lo = min(lo, (hde ? de.lo : 1) - 1);  hi = max(hi, (hde ? de.hi : -1) - 1);
-  const bool ai = ho || hie, ad = ho || hde;
-  const int width = hi - lo + 1;
-  WfRef om, oi, od;
-  int offm = 0, offi = 0, offd = 0, need = 0;
-  if (!c.leaf) {
-    if (width > c.W) return false;
-    om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
-    oi.base = om.base + c.W;
-    od.base = oi.base + c.W;
-    om.kbase = oi.kbase = od.kbase = 0;
-    om.mask = oi.mask = od.mask = (uint32_t)c.W - 1u;
-  } else {
-    need = width * (1 + (ai ? 1 : 0) + (ad ? 1 : 0));
-    if (used + need > d.lcap) return false;
-    offm = used;
-    offi = offm + width;
-    offd = offi + (ai ? width : 0);
-    om.base = c.ldata + offm; oi.base = c.ldata + offi; od.base = c.ldata + offd;
-    om.kbase = oi.kbase = od.kbase = lo;
-    om.mask = oi.mask = od.mask = 0xffffffffu;
-  }
-  int r[6] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};  // M, I, D trimmed lo/hi
-  for (int k = lo + g.tid; k <= hi; k += 32 * G) {
-    const int32_t ins = max(mo.get(k - 1), ie.get(k - 1)) + 1;
-    const int32_t del = max(mo.get(k + 1), de.get(k + 1));
-    const int32_t mis = mx.get(k) + 1;
-    int32_t m = max(del, max(mis, ins));
-    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
-    om.put(k, m);
-    if (m != kNull) { r[0] = min(r[0], k); r[1] = max(r[1], k); }
-    if (ai) {
-      oi.put(k, ins);
-      if ((uint32_t)ins <= tl && (uint32_t)(ins - k) <= pl) { r[2] = min(r[2], k); r[3] = max(r[3], k); }
-    }
-    if (ad) {
-      od.put(k, del);
-      if ((uint32_t)del <= tl && (uint32_t)(del - k) <= pl) { r[4] = min(r[4], k); r[5] = max(r[5], k); }
-    }
-  }
-  // Trim both ends of every output (wavefront_compute_trim_ends): the surviving range is
-  // [min in-bounds k, max in-bounds k]; none in bounds leaves a null wavefront.
-  const bool mm[6] = {false, true, false, true, false, true};
-  g.minmax(r, mm);
-  g.sync();
-  d.num_null = 0;
-  if (c.leaf) d.lused = used + need;
-  else { c.rphys[slot_of(c, s)] = nphys; d.next_phys = (nphys + 1 == c.nphys) ? 0 : nphys + 1; }
-  if (r[0] <= r[1]) set_desc(c, s, 0, r[0], r[1], offm, lo); else set_desc(c, s, 0, lo, lo - 1, offm, lo);
-  if (ai) { if (r[2] <= r[3]) set_desc(c, s, 1, r[2], r[3], offi, lo); else set_desc(c, s, 1, lo, lo - 1, offi, lo); }
-  else set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
-  if (ad) { if (r[4] <= r[5]) set_desc(c, s, 2, r[4], r[5], offd, lo); else set_desc(c, s, 2, lo, lo - 1, offd, lo); }
-  else set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
-  return true;
-}
-
 // wavefront_extend_end2end(_max) + wavefront_termination_end2end. Returns 1 when the
 // direction is finished (end reached or unreachable).
 template <int G>
@@ -387,25 +335,47 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   }
   // r: M, I, D trimmed lo/hi, then the max antidiagonal of the extended M
   int r[7] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN, 0};
-  for (int k = lo + g.tid; k <= hi; k += 32 * G) {
-    const int32_t ins = max(mo.get(k - 1), ie.get(k - 1)) + 1;
-    const int32_t del = max(mo.get(k + 1), de.get(k + 1));
-    const int32_t mis = mx.get(k) + 1;
-    int32_t m = max(del, max(mis, ins));
-    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
-    if (m != kNull) {
-      r[0] = min(r[0], k); r[1] = max(r[1], k);
-      m += lcp(sv, m - k, m);
-      r[6] = max(r[6], 2 * m - k);
+  // U diagonals per thread per iteration, so that their loads are in flight together. For
+  // k > hi every input read falls outside its input's [lo, hi] (the output range covers
+  // them), so those lanes read nothing and store nothing.
+  constexpr int U = kStepUnroll;
+  for (int kb = lo + g.tid; kb <= hi; kb += U * 32 * G) {
+    int32_t mv[U], iv[U], dv[U];
+    uint32_t xw[U];
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = kb + u * 32 * G;
+      iv[u] = max(mo.get(k - 1), ie.get(k - 1)) + 1;
+      dv[u] = max(mo.get(k + 1), de.get(k + 1));
+      int32_t m = max(dv[u], max(mx.get(k) + 1, iv[u]));
+      if (k > hi || (uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
+      mv[u] = m;
     }
-    om.put(k, m);
-    if (ai) {
-      oi.put(k, ins);
-      if ((uint32_t)ins <= tl && (uint32_t)(ins - k) <= pl) { r[2] = min(r[2], k); r[3] = max(r[3], k); }
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = kb + u * 32 * G;
+      xw[u] = (mv[u] != kNull) ? lcp_first(sv, mv[u] - k, mv[u]) : 1u;
     }
-    if (ad) {
-      od.put(k, del);
-      if ((uint32_t)del <= tl && (uint32_t)(del - k) <= pl) { r[4] = min(r[4], k); r[5] = max(r[5], k); }
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = kb + u * 32 * G;
+      if (k > hi) break;
+      int32_t m = mv[u];
+      if (m != kNull) {
+        r[0] = min(r[0], k); r[1] = max(r[1], k);
+        m += lcp_rest(sv, m - k, m, xw[u]);
+        r[6] = max(r[6], 2 * m - k);
+      }
+      om.put(k, m);
+      const int32_t ins = iv[u], del = dv[u];
+      if (ai) {
+        oi.put(k, ins);
+        if ((uint32_t)ins <= tl && (uint32_t)(ins - k) <= pl) { r[2] = min(r[2], k); r[3] = max(r[3], k); }
+      }
+      if (ad) {
+        od.put(k, del);
+        if ((uint32_t)del <= tl && (uint32_t)(del - k) <= pl) { r[4] = min(r[4], k); r[5] = max(r[5], k); }
+      }
     }
   }
   const bool mm[7] = {false, true, false, true, false, true, true};
@@ -990,7 +960,7 @@ cudaError_t launch_shape(const KernelParams& p, int grid, cudaStream_t stream) {
 int biwfa_warps_per_block() { return 4; }
 
 cudaError_t biwfa_occupancy(int* blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<1, 4, false, 6>,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<1, 4, false, kMinBlocksPerSM>,
                                                        4 * 32, 0);
 }
 
@@ -1002,7 +972,7 @@ int biwfa_groups_per_block(int group_warps, int ring_in_smem) {
 
 cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream) {
   const int gw = p.group_warps > 0 ? p.group_warps : 1;
-  if (gw == 1) return launch_shape<1, 4, false, 6>(p, grid, stream);
+  if (gw == 1) return launch_shape<1, 4, false, kMinBlocksPerSM>(p, grid, stream);
   if (gw == 8) {
     if (p.ring_in_smem) return launch_shape<8, 1, true, 1>(p, grid, stream);
     return launch_shape<8, 1, false, 2>(p, grid, stream);

@@ -93,16 +93,11 @@ wavefront_aligner_attr_t wavefront_aligner_attr_default = {
     {INT_MAX, 3000, 6000, 0, (uint64_t)-1, (uint64_t)-1, UINT64_MAX, 0, false, 1, 500},
 };
 
+// The GPU context is created by the first alignment (device WFG_DEVICE, default 0), so an
+// aligner exists, and reports its configuration errors, on a machine without a GPU.
 wavefront_aligner_t* wavefront_aligner_new(wavefront_aligner_attr_t* attributes) {
   if (attributes == NULL) attributes = &wavefront_aligner_attr_default;
-  const char* dev = getenv("WFG_DEVICE");
-  wfg_context_t* ctx = wfg_context_create(dev ? atoi(dev) : 0);
-  if (ctx == NULL) {
-    fprintf(stderr, "[WFA-GB300] no usable CUDA device\n");
-    return NULL;
-  }
   AlignerImpl* im = new AlignerImpl();
-  im->ctx = ctx;
   im->attr = *attributes;
   check_config(im);
   wavefront_aligner_t* wf = (wavefront_aligner_t*)calloc(1, sizeof(wavefront_aligner_t));
@@ -120,7 +115,7 @@ wavefront_aligner_t* wavefront_aligner_new(wavefront_aligner_attr_t* attributes)
 void wavefront_aligner_delete(wavefront_aligner_t* const wf) {
   if (!wf) return;
   AlignerImpl* im = impl_of(wf);
-  wfg_context_destroy(im->ctx);
+  if (im->ctx) wfg_context_destroy(im->ctx);
   delete im;
   free(wf->cigar);
   free(wf);
@@ -152,6 +147,16 @@ int wavefront_align_batch(wavefront_aligner_t* const wf, const int n, const char
     for (int i = 0; i < n; ++i) { if (scores) scores[i] = 0; if (statuses) statuses[i] = WF_STATUS_UNSUPPORTED; }
     wf->align_status.status = WF_STATUS_UNSUPPORTED;
     return WF_STATUS_UNSUPPORTED;
+  }
+  if (im->ctx == NULL) {
+    const char* dev = getenv("WFG_DEVICE");
+    im->ctx = wfg_context_create(dev ? atoi(dev) : 0);
+    if (im->ctx == NULL) {
+      fprintf(stderr, "[WFA-GB300] no usable CUDA device\n");
+      for (int i = 0; i < n; ++i) { if (scores) scores[i] = 0; if (statuses) statuses[i] = WF_STATUS_DEVICE_ERROR; }
+      wf->align_status.status = WF_STATUS_DEVICE_ERROR;
+      return WF_STATUS_DEVICE_ERROR;
+    }
   }
   int64_t total = 0;
   for (int i = 0; i < n; ++i) total += (int64_t)plens[i] + tlens[i];

@@ -133,6 +133,10 @@ struct wfg_context {
     float ring_margin = 1.4f;       // ring width = margin * predicted score / e + 64
   } tune;
   cudaStream_t aux_stream = nullptr;
+  // wfg_run's device work as a CUDA graph (wfg_set_graph)
+  int use_graph = 1;
+  cudaGraphExec_t graph_exec = nullptr;
+  wfg::PinBuf<int> h_order_pin;  // the processing order, copied by the graph's first node
 };
 
 int wfg_fail(wfg_context* c, cudaError_t e, const char* where);

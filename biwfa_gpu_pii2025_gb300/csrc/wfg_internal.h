@@ -95,7 +95,7 @@ WFG_HD constexpr inline int wfg_ring_buffers(int x, int o, int e) {
 
 // Per-warp arena carving (bytes); all offsets 256-byte aligned.
 struct ArenaLayout {
-  int64_t ring_off, ring_bytes;     // 2 directions x scope x 3 components x ring_w int32
+  int64_t ring_off, ring_bytes;     // 2 directions x buffers x 3 components x ring_w int32
   int64_t ldesc_off, ldesc_bytes;   // (leaf_max_score+1) x 3 x int4
   int64_t ldata_off, ldata_bytes;   // leaf_words int32
   int64_t runs_off, runs_bytes;     // run_cap uint32

@@ -73,6 +73,8 @@ void wfg_context_destroy(wfg_context_t* c) {
   c->d_runoff.release(); c->d_runs.release(); c->d_counters.release(); c->d_arena.release();
   c->d_flush.release(); c->h_counters.release(); c->h_pairs_pinned.release();
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  c->h_order_pin.release();
   cudaStreamDestroy(c->stream);
   cudaStreamDestroy(c->aux_stream);
   delete c;
@@ -365,11 +367,11 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     arena_need = std::max(arena_need, l.groups * l.L.total);
   }
   WFG_CHECK(c, c->d_arena.reserve((size_t)arena_need));
-  if (n > 0) WFG_CHECK(c, cudaMemcpyAsync(c->d_order.ptr, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
-  WFG_CHECK(c, cudaEventRecord(c->ev[0], c->stream));
-  WFG_CHECK(c, cudaMemsetAsync(c->d_counters.ptr, 0, sizeof(unsigned long long) * kNumCounters, c->stream));
-  WFG_CHECK(c, launch_pack(n, c->d_seq.ptr, c->d_pairs.ptr, c->d_words.ptr, c->num_sms, c->stream));
-  WFG_CHECK(c, cudaEventRecord(c->ev[1], c->stream));
+  // The order goes through a pinned buffer (a graph's copy node reads it when the graph
+  // runs): wait until the previous run's copy of it is done before overwriting it.
+  if (c->ran) WFG_CHECK(c, cudaEventSynchronize(c->ev[0]));
+  WFG_CHECK(c, c->h_order_pin.reserve((size_t)std::max(n, 1)));
+  if (n > 0) std::copy(order.begin(), order.end(), c->h_order_pin.ptr);
   auto params = [&](const Launch& l, int ps) {
     KernelParams kp{};
     kp.x = p.x; kp.o = p.o; kp.e = p.e; kp.scope = p.scope;
@@ -401,51 +403,99 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     kp.retry_count = c->d_counters.ptr + ps * kCountersPerPass + 1;
     return kp;
   };
-  int launches = 1;
-  // pass 0: the first launch on the context's stream, a second one (wide pairs) on the aux
-  // stream, joined before the retry passes
-  for (size_t li = 0; li < first.size(); ++li) {
-    const Launch& l = first[li];
-    KernelParams kp = params(l, 0);
-    kp.num_pairs = l.count;
-    kp.num_pairs_ptr = nullptr;
-    kp.order = c->d_order.ptr + l.order_off;
-    kp.queue_head = c->d_counters.ptr + (li == 0 ? 0 : 2);
-    cudaStream_t st = c->stream;
-    if (li > 0) {
-      WFG_CHECK(c, cudaStreamWaitEvent(c->aux_stream, c->ev[1], 0));
-      st = c->aux_stream;
+  int launches = 0;
+  // The device work of one run. Timing events are external record nodes when captured;
+  // ev[5] / ev[4] fork the aux stream off and join it back (capture dependencies).
+  auto enqueue = [&](bool capturing) -> cudaError_t {
+    auto mark = [&](cudaEvent_t ev) {
+      return capturing ? cudaEventRecordWithFlags(ev, c->stream, cudaEventRecordExternal) : cudaEventRecord(ev, c->stream);
+    };
+    cudaError_t e = cudaSuccess;
+    launches = 1;
+    if (n > 0 && (e = cudaMemcpyAsync(c->d_order.ptr, c->h_order_pin.ptr, sizeof(int) * (size_t)n,
+                                      cudaMemcpyHostToDevice, c->stream)) != cudaSuccess) return e;
+    if ((e = mark(c->ev[0])) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c->d_counters.ptr, 0, sizeof(unsigned long long) * kNumCounters, c->stream)) != cudaSuccess)
+      return e;
+    if ((e = launch_pack(n, c->d_seq.ptr, c->d_pairs.ptr, c->d_words.ptr, c->num_sms, c->stream)) != cudaSuccess) return e;
+    if ((e = mark(c->ev[1])) != cudaSuccess) return e;
+    // pass 0: the first launch on the context's stream, a second one (wide pairs) on the aux
+    // stream, joined before the retry passes
+    for (size_t li = 0; li < first.size(); ++li) {
+      const Launch& l = first[li];
+      if (l.count <= 0) continue;
+      KernelParams kp = params(l, 0);
+      kp.num_pairs = l.count;
+      kp.num_pairs_ptr = nullptr;
+      kp.order = c->d_order.ptr + l.order_off;
+      kp.queue_head = c->d_counters.ptr + (li == 0 ? 0 : 2);
+      cudaStream_t st = c->stream;
+      if (li > 0) {
+        if ((e = cudaEventRecord(c->ev[5], c->stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(c->aux_stream, c->ev[5], 0)) != cudaSuccess) return e;
+        st = c->aux_stream;
+      }
+      if ((e = launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), st)) != cudaSuccess) return e;
+      ++launches;
+      if (li > 0) {
+        if ((e = cudaEventRecord(c->ev[4], c->aux_stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(c->stream, c->ev[4], 0)) != cudaSuccess) return e;
+      }
     }
-    if (l.count > 0) {
-      WFG_CHECK(c, launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), st));
+    if ((e = mark(c->ev[2])) != cudaSuccess) return e;
+    for (int ps = 1; ps < kNumPasses; ++ps) {
+      const Launch& l = retry[ps];
+      if (n <= 0) break;
+      KernelParams kp = params(l, ps);
+      kp.num_pairs = n;
+      kp.num_pairs_ptr = c->d_counters.ptr + (ps - 1) * kCountersPerPass + 1;
+      kp.order = c->d_retry.ptr + (size_t)(ps - 1) * n;
+      kp.queue_head = c->d_counters.ptr + ps * kCountersPerPass + 0;
+      if ((e = launch_biwfa(kp, (int)(l.groups / 4), c->stream)) != cudaSuccess) return e;
       ++launches;
     }
-    if (li > 0) {
-      WFG_CHECK(c, cudaEventRecord(c->ev[4], c->aux_stream));
-      WFG_CHECK(c, cudaStreamWaitEvent(c->stream, c->ev[4], 0));
+    if ((e = mark(c->ev[3])) != cudaSuccess) return e;
+    return cudaMemcpyAsync(c->h_counters.ptr, c->d_counters.ptr, sizeof(unsigned long long) * kNumCounters,
+                           cudaMemcpyDeviceToHost, c->stream);
+  };
+  c->stats.used_graph = 0;
+  if (c->use_graph) {
+    WFG_CHECK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t e = enqueue(true);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(c->stream, &graph);
+    if (e != cudaSuccess || ec != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return wfg_fail(c, e != cudaSuccess ? e : ec, "wfg_run graph capture");
     }
-  }
-  WFG_CHECK(c, cudaEventRecord(c->ev[2], c->stream));
-  for (int ps = 1; ps < kNumPasses; ++ps) {
-    const Launch& l = retry[ps];
-    KernelParams kp = params(l, ps);
-    kp.num_pairs = n;
-    kp.num_pairs_ptr = c->d_counters.ptr + (ps - 1) * kCountersPerPass + 1;
-    kp.order = c->d_retry.ptr + (size_t)(ps - 1) * n;
-    kp.queue_head = c->d_counters.ptr + ps * kCountersPerPass + 0;
-    if (n > 0) {
-      WFG_CHECK(c, launch_biwfa(kp, (int)(l.groups / 4), c->stream));
-      ++launches;
+    if (c->graph_exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(c->graph_exec, graph, &info) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = nullptr;
+      }
     }
+    cudaError_t ei = cudaSuccess;
+    if (!c->graph_exec) ei = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    WFG_CHECK(c, ei);
+    WFG_CHECK(c, cudaGraphLaunch(c->graph_exec, c->stream));
+    c->stats.used_graph = 1;
+  } else {
+    WFG_CHECK(c, enqueue(false));
   }
-  WFG_CHECK(c, cudaEventRecord(c->ev[3], c->stream));
-  WFG_CHECK(c, cudaMemcpyAsync(c->h_counters.ptr, c->d_counters.ptr, sizeof(unsigned long long) * kNumCounters,
-                               cudaMemcpyDeviceToHost, c->stream));
   c->stats.launches = launches;
   c->stats.num_warps = (int)(first[0].groups * first[0].gw);
   c->stats.ring_w = first[0].ring_w;
   c->stats.arena_bytes = first[0].L.total;
   c->ran = true;
+  return WF_STATUS_ALG_COMPLETED;
+}
+
+int wfg_set_graph(wfg_context_t* c, int enable) {
+  if (!c) return WF_STATUS_UNSUPPORTED;
+  c->use_graph = enable ? 1 : 0;
   return WF_STATUS_ALG_COMPLETED;
 }
 

@@ -236,6 +236,7 @@ typedef struct {
   int64_t arena_bytes;    /* per-warp arena of the main launch */
   int64_t total_runs;     /* CIGAR runs produced */
   int64_t h2d_bytes, d2h_bytes; /* bytes copied by the last upload / fetch */
+  int used_graph;         /* 1 when the last wfg_run's device work ran as one CUDA graph */
 } wfg_stats_t;
 
 wfg_context_t* wfg_context_create(int device);
@@ -275,6 +276,11 @@ int wfg_set_arena_limits(wfg_context_t* ctx, int ring_w, int leaf_words);
  * shared memory (group_warps > 1; rings of 1024 diagonals, wider pairs overflow into the
  * retry passes). Results never depend on the shape. Default 1, 0. */
 int wfg_set_exec_shape(wfg_context_t* ctx, int group_warps, int ring_in_smem);
+/* Run wfg_run's device work (order copy, counter reset, packing, every pass, counter
+ * read-back) as one CUDA graph: captured on each call and applied to the context's
+ * instantiated graph with cudaGraphExecUpdate when the topology is unchanged. enable = 0
+ * issues the same work directly on the streams. Default 1. */
+int wfg_set_graph(wfg_context_t* ctx, int enable);
 /* Policy of WFG_SCHED_LEARNED: pairs whose predicted score is at least wide_threshold run
  * with wide_warps warps per pair (rings in shared memory when wide_smem and they fit),
  * concurrently with the single-warp launch for the rest; ring widths are
@@ -328,7 +334,8 @@ int wfg_model_gradient(wfg_model_t* model, wfg_context_t* ctx, const float* log_
 /* Predicted scores of the resident batch (kept on the device for WFG_SCHED_LEARNED;
  * optionally copied to host_pred). */
 int wfg_model_predict(wfg_model_t* model, wfg_context_t* ctx, float* host_pred);
-/* Attach a model to a context: WFG_SCHED_LEARNED then predicts on the device in wfg_run. */
+/* Attach a model to a context: WFG_SCHED_LEARNED then predicts on the device in wfg_run.
+ * The context keeps the pointer: attach NULL before destroying the model. */
 int wfg_set_model(wfg_context_t* ctx, wfg_model_t* model);
 
 /* Aligning without allocating (no WFA2-lib counterpart; there is no reference interface

@@ -106,6 +106,71 @@ def test_given_order_and_predictions_do_not_change_results(batch_aligner):
             assert np.array_equal(r.runs_of(i), ref.runs_of(i))
 
 
+def test_graph_and_direct_launches_agree(batch_aligner):
+    """wfg_run's device work as a captured CUDA graph (updated in place across batches of
+    different sizes and schedules) gives the results of direct launches."""
+    outs = {}
+    for graph in (True, False):
+        batch_aligner.set_graph(graph)
+        try:
+            for n, seed in ((120, 5), (37, 6), (120, 7)):
+                b = pkg.PairBatch.generate(5, n, seed=seed)
+                for sched in (_capi.SCHED_PLAIN, _capi.SCHED_LEARNED):
+                    batch_aligner.upload(b)
+                    if sched == _capi.SCHED_LEARNED:
+                        batch_aligner.set_predictions(np.asarray(b.plen, np.float32) * 0.3)
+                    batch_aligner.run(sched=sched)
+                    st = batch_aligner.stats()
+                    assert st.used_graph == int(graph)
+                    outs[(graph, n, seed, sched)] = batch_aligner.fetch()
+        finally:
+            batch_aligner.set_graph(True)
+    for (graph, n, seed, sched), r in outs.items():
+        d = outs[(False, n, seed, sched)]
+        assert (r.status == 0).all()
+        assert np.array_equal(r.scores, d.scores)
+        for i in range(n):
+            assert np.array_equal(r.runs_of(i), d.runs_of(i))
+
+
+def _mutate(rng, seq: bytes, n_edits: int) -> bytes:
+    s = bytearray(seq)
+    for _ in range(n_edits):
+        i = int(rng.integers(0, len(s)))
+        kind = int(rng.integers(0, 3))
+        if kind == 0:
+            s[i] = b"ACGT"[(b"ACGT".index(s[i]) + 1 + int(rng.integers(0, 3))) % 4]
+        elif kind == 1:
+            s.insert(i, b"ACGT"[int(rng.integers(0, 4))])
+        else:
+            del s[i]
+    return bytes(s)
+
+
+def test_long_low_error_pairs_match_oracle(batch_aligner):
+    """Long pairs (up to 32 kbp) with long exact runs between edits: deep LCP loops, three
+    recursion levels, and the same results through the tiny-arena retry passes."""
+    rng = np.random.default_rng(77)
+    pats, txts = [], []
+    for L in (32766, 32000, 20000, 8000):
+        p = bytes(rng.choice(list(b"ACGT"), L).astype(np.uint8))
+        pats.append(p)
+        txts.append(_mutate(rng, p, L // 200)[:32766])
+    b = pkg.PairBatch.from_lists(pats, txts)
+    res = batch_aligner.align(b)
+    try:
+        batch_aligner.set_arena_limits(ring_w=32, leaf_words=256)
+        small = batch_aligner.align(b)
+    finally:
+        batch_aligner.set_arena_limits(0, 0)
+    for i in range(b.n):
+        st, score, ops, _ = binding.oracle_align(pats[i], txts[i])
+        assert st == 0 and res.status[i] == 0 and small.status[i] == 0
+        assert res.scores[i] == score and small.scores[i] == score
+        assert pkg.runs_to_ops(res.runs_of(i)) == ops
+        assert np.array_equal(small.runs_of(i), res.runs_of(i))
+
+
 def test_wfa2_single_pair_api():
     data = utest()
     s = data["sets"]["test.biwfa.affine.alg"]
