@@ -258,7 +258,7 @@ def train_predictor(pkg, al, wl: int, n_train: int, rank: int):
     losses = pred.train(-scores, epochs=20, batch_rows=4096, lr=3e-3, seed=5)
     train_s = time.perf_counter() - t0
     # the autotuner measures on a held-out slice of the same generator (another seed)
-    tune_n = min(n_train, 60_000)
+    tune_n = min(n_train, 200_000)
     al.upload(pkg.PairBatch.generate(wl, tune_n, TRAIN_SEED + 1 + 7919 * rank))
     pred.attach()
     tuned = al.autotune_learned_policy(PENALTIES)
@@ -309,12 +309,16 @@ def run_ours(args):
     al.upload(batch)
     if learned:
         pred.attach()
-    # ---- plain length-sorted path (the comparison), then the learned-binned path (value)
+    # ---- the plain length-sorted batched path (the comparison: one launch per resident set of
+    # pairs, each waiting for its slowest pair), the length-sorted persistent path (ablation:
+    # work stealing without the predictor), then the learned-binned persistent path (value)
     plain_ms, plain_kernel_ms, _, _ = time_path(al, _capi.SCHED_PLAIN, args.steps, args.warmup, dist)
     plain_res = al.fetch()
+    sorted_ms, _, _, _ = time_path(al, _capi.SCHED_SORTED, args.steps, args.warmup, dist)
     sched = _capi.SCHED_LEARNED if learned else _capi.SCHED_PLAIN
-    sched_name = ("learned-binned (MLP score prediction; autotuned warps-per-pair and shared-memory rings)"
-                  if learned else "plain (length-sorted, one arena size)")
+    sched_name = ("learned-binned persistent (MLP score prediction orders and bins pairs, sizes scratch; "
+                  "autotuned warps-per-pair and shared-memory rings)"
+                  if learned else "plain length-sorted batched launches")
     step_ms, kernel_ms, launches, clk = time_path(al, sched, args.steps, args.warmup, dist,
                                                   ClockSampler(local if world > 1 else 0))
     res = al.fetch()
@@ -324,6 +328,7 @@ def run_ours(args):
     total_runs = int(res.runs.shape[0])
     t_step = dist.max(statistics.mean(step_ms))
     t_plain = dist.max(statistics.mean(plain_ms))
+    t_sorted = dist.max(statistics.mean(sorted_ms))
     pairs_all = dist.sum(float(n))
     value = pairs_all / (t_step / 1e3)
     cells = float((batch.plen.astype(np.float64) * batch.tlen).sum())
@@ -366,6 +371,8 @@ def run_ours(args):
             "gcups": gcups, "pairs_ok": ok,
             "plain_value": pairs_all / (t_plain / 1e3), "plain_ms_per_step": t_plain,
             "learned_over_plain": (t_plain / t_step) if learned else None,
+            "sorted_persistent_value": pairs_all / (t_sorted / 1e3), "sorted_persistent_ms_per_step": t_sorted,
+            "learned_over_sorted_persistent": (t_sorted / t_step) if learned else None,
             "results_identical_to_plain": same_as_plain,
             "learned": learn_info,
             "e2e": {"value": dist.sum(float(n)) / (e2e_t / 1e3), "unit": "pairs/s", "h2d_bytes_per_step": h2d,
@@ -387,6 +394,32 @@ def run_ours(args):
     return 0
 
 
+SCHEDS = {"plain": 0, "learned": 1, "sorted": 3}
+
+
+def run_profile_case(args):
+    """A bare run of one schedule for ncu: warmup + steps runs of the resident batch. The
+    learned schedule trains its predictor first (as the timed bench does)."""
+    import biwfa_gpu_pii2025_gb300 as pkg
+    wl = args.workload
+    n = args.pairs or WORKLOADS[wl][1]
+    al = pkg.BatchAligner(0)
+    pred = None
+    if args.profile_sched == "learned":
+        pred, _ = train_predictor(pkg, al, wl, min(200_000, max(n, 2000)), 0)
+    al.upload(make_batch(wl, n, 0))
+    if pred is not None:
+        pred.attach()
+    for _ in range(args.warmup + args.steps):
+        al.run(PENALTIES, sched=SCHEDS[args.profile_sched])
+        al.synchronize()
+    res = al.fetch()
+    print(json.dumps({"profile_sched": args.profile_sched, "workload": wl, "pairs": n,
+                      "runs": args.warmup + args.steps, "pairs_ok": int((res.status == 0).sum())}))
+    al.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -397,11 +430,16 @@ def main():
     ap.add_argument("--pairs", type=int, default=0, help="override the workload's pair count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time only the plain length-sorted path")
+    ap.add_argument("--profile-sched", choices=sorted(SCHEDS), default=None,
+                    help="no timing: upload the batch, run the schedule warmup + steps times and exit "
+                         "(the command the ncu captures in profiles/ run)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_sched:
+        return run_profile_case(args)
     return run_ours(args)
 
 

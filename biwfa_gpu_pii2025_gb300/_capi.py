@@ -25,7 +25,7 @@ COMPUTE_SCORE, COMPUTE_ALIGNMENT = 0, 1
 ALIGNMENT_END2END, ALIGNMENT_ENDSFREE = 0, 1
 WF_HEURISTIC_NONE, WF_HEURISTIC_WFADAPTIVE = 0, 4
 WAVEFRONT_MEMORY_HIGH, WAVEFRONT_MEMORY_ULTRALOW = 0, 3
-SCHED_PLAIN, SCHED_LEARNED, SCHED_GIVEN = 0, 1, 2
+SCHED_PLAIN, SCHED_LEARNED, SCHED_GIVEN, SCHED_SORTED = 0, 1, 2, 3
 
 # SAM op codes of the output runs
 OP_INS, OP_DEL, OP_EQ, OP_X = 1, 2, 7, 8
@@ -138,6 +138,7 @@ SIGNATURES = {
     "wfg_set_arena_limits": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "wfg_set_exec_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "wfg_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "wfg_set_retry_shape": (C.c_int, [C.c_void_p, C.c_int]),
     "wfg_set_learned_policy": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_float]),
     "wfg_autotune_learned_policy": (C.c_int, [C.c_void_p, P(Config), P(C.c_float), P(C.c_float), _ip, _ip]),
     "wfg_flush_l2": (C.c_int, [C.c_void_p, C.c_int64]),

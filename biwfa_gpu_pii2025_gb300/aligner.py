@@ -183,6 +183,10 @@ class BatchAligner:
         """Run each wfg_run's device work as one CUDA graph (default) or as direct launches."""
         self._check(self.lib.wfg_set_graph(self.ctx, 1 if enable else 0), "wfg_set_graph")
 
+    def set_retry_shape(self, group_warps: int = 8):
+        """Warps per pair of the retry passes (default 8)."""
+        self._check(self.lib.wfg_set_retry_shape(self.ctx, group_warps), "wfg_set_retry_shape")
+
     def set_learned_policy(self, wide_threshold=1200.0, wide_warps=8, wide_smem=True, ring_margin=1.4):
         self._check(self.lib.wfg_set_learned_policy(self.ctx, wide_threshold, wide_warps, 1 if wide_smem else 0,
                                                     ring_margin), "wfg_set_learned_policy")
@@ -201,7 +205,7 @@ class BatchAligner:
         self._check(self.lib.wfg_set_predictions(self.ctx, pred.ctypes.data_as(C.POINTER(C.c_float))),
                     "wfg_set_predictions")
 
-    def run(self, penalties=(0, 4, 6, 2), score_only=False, sched=_capi.SCHED_PLAIN, max_steps=0):
+    def run(self, penalties=(0, 4, 6, 2), score_only=False, sched=_capi.SCHED_SORTED, max_steps=0):
         cfg = self.config(penalties, score_only, max_steps)
         self._check(self.lib.wfg_run(self.ctx, C.byref(cfg), sched), "wfg_run")
 
@@ -234,7 +238,7 @@ class BatchAligner:
         self.n = b.n
         return int(total.value)
 
-    def align(self, b: PairBatch, penalties=(0, 4, 6, 2), score_only=False, sched=_capi.SCHED_PLAIN,
+    def align(self, b: PairBatch, penalties=(0, 4, 6, 2), score_only=False, sched=_capi.SCHED_SORTED,
               max_steps=0) -> BatchResult:
         self.upload(b)
         self.run(penalties, score_only, sched, max_steps)

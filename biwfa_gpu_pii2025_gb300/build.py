@@ -24,7 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
 SOURCES = ["biwfa_kernel.cu", "wfg_runtime.cpp", "wfa2_compat.cpp", "datagen.cpp", "noalloc.cu", "mlp_kernel.cu",
-           "wfg_model.cpp", "autotune.cpp"]
+           "wfg_model.cpp", "autotune.cpp",
+           "sched_kernel.cu"]
 
 
 def nvcc_path() -> str:

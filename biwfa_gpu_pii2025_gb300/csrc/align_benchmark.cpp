@@ -161,7 +161,7 @@ int main(int argc, char** argv) {
     runs.resize(b.seq.size() + (size_t)n + 16);  // a CIGAR has at most |P| + |T| runs
     int64_t nruns = 0;
     const auto t0 = std::chrono::steady_clock::now();
-    const int st = wfg_align_host(ctx, &cfg, WFG_SCHED_PLAIN, n, b.seq.data(), (int64_t)b.seq.size(), b.p_off.data(),
+    const int st = wfg_align_host(ctx, &cfg, WFG_SCHED_SORTED, n, b.seq.data(), (int64_t)b.seq.size(), b.p_off.data(),
                                   b.plen.data(), b.t_off.data(), b.tlen.data(), scores.data(), statuses.data(),
                                   run_off.data(), run_len.data(), runs.data(), (int64_t)runs.size(), &nruns);
     align_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

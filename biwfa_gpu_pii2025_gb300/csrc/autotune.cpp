@@ -1,7 +1,8 @@
-// Autotuner of the learned schedule: which pairs run with several warps per pair (and with
-// their rings in shared memory) is a trade-off between per-pair latency and the number of
-// pairs in flight that depends on the batch, so it is measured rather than modelled. Each
-// candidate policy runs the resident batch once (after one warm-up run); the fastest is kept.
+// Autotuner of the learned schedule: whether the heaviest predicted pairs (at most one
+// resident wave of the multi-warp shape, from a predicted-score threshold up) run with several
+// warps per pair, and with their rings in shared memory, trades per-pair latency against pairs
+// in flight and depends on the batch, so it is measured rather than modelled. Each candidate
+// policy runs the resident batch twice; the time of the second run decides.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -16,7 +17,7 @@ extern "C" int wfg_autotune_learned_policy(wfg_context_t* c, const wfg_config_t*
   struct Cand { float thr; int gw; int smem; };
   std::vector<Cand> cands;
   cands.push_back({FLT_MAX, 8, 0});  // no wide launch
-  for (float thr : {300.f, 600.f, 1200.f, 2400.f}) {
+  for (float thr : {1200.f, 2400.f, 4800.f}) {
     cands.push_back({thr, 8, 1});
     cands.push_back({thr, 8, 0});
     cands.push_back({thr, 4, 0});

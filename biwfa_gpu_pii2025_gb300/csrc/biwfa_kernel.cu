@@ -197,10 +197,13 @@ __device__ __forceinline__ int slot_of(const DirCfg& c, int score) {
   return score - c.scope * (int)__umulhi((uint32_t)score, c.magic);
 }
 
+// MODE: 0 ring, 1 leaf store, -1 read from the configuration (callers that serve both).
+template <int MODE = -1>
 __device__ __forceinline__ WfRef ref_raw(const DirCfg& c, int score, int ci) {
   if (score < 0) return absent_ref();
   WfRef r;
-  if (!c.leaf) {
+  const bool leaf = MODE < 0 ? (c.leaf != 0) : (MODE == 1);
+  if (!leaf) {
     const int slot = slot_of(c, score);
     const int2 ds = c.rdesc[slot * 3 + ci];
     r.lo = ds.x; r.hi = ds.y;
@@ -217,12 +220,15 @@ __device__ __forceinline__ WfRef ref_raw(const DirCfg& c, int score, int ci) {
 }
 // Input fetch: absent when the score is negative, the slot is empty or the wavefront is
 // null (wavefront_compute_get_*wavefront).
+template <int MODE = -1>
 __device__ __forceinline__ WfRef fetch(const DirCfg& c, int score, int ci) {
-  const WfRef r = ref_raw(c, score, ci);
+  const WfRef r = ref_raw<MODE>(c, score, ci);
   return r.nonnull() ? r : absent_ref();
 }
+template <int MODE = -1>
 __device__ __forceinline__ void set_desc(const DirCfg& c, int score, int ci, int lo, int hi, int data_off, int kbase) {
-  if (!c.leaf) c.rdesc[slot_of(c, score) * 3 + ci] = make_int2(lo, hi);
+  const bool leaf = MODE < 0 ? (c.leaf != 0) : (MODE == 1);
+  if (!leaf) c.rdesc[slot_of(c, score) * 3 + ci] = make_int2(lo, hi);
   else c.ldesc[score * 3 + ci] = make_int4(lo, hi, data_off, kbase);
 }
 
@@ -285,26 +291,27 @@ __device__ __noinline__ int dir_extend(Dir& d, int s, const Grp<G> g, int* max_a
 // range is fixed by which M[k] are in bounds before extension, so the extended offset is
 // written once. Returns -1 on scratch overflow, 1 when the direction is finished (end
 // reached or unreachable), 0 otherwise; *max_ak receives the extension's max antidiagonal.
-template <int G>
+template <int G, int MODE>
 __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g, int* max_ak_out) {
   const DirCfg c = d.cfg;
+  constexpr bool kLeaf = MODE == 1;  // the leaf store (else the modular rings)
   const int nn = d.num_null, used = d.lused, nphys = d.next_phys, ce = d.ce;
   const SeqView sv = d.sv;
   const uint32_t tl = (uint32_t)sv.tlen, pl = (uint32_t)sv.plen;
   *max_ak_out = 0;
-  if (c.leaf && s > c.lmax) return -1;
-  const WfRef mx = fetch(c, s - p.x, 0);
-  const WfRef mo = fetch(c, s - p.o - p.e, 0);
-  const WfRef ie = fetch(c, s - p.e, 1);
-  const WfRef de = fetch(c, s - p.e, 2);
+  if (kLeaf && s > c.lmax) return -1;
+  const WfRef mx = fetch<MODE>(c, s - p.x, 0);
+  const WfRef mo = fetch<MODE>(c, s - p.o - p.e, 0);
+  const WfRef ie = fetch<MODE>(c, s - p.e, 1);
+  const WfRef de = fetch<MODE>(c, s - p.e, 2);
   const bool hx = mx.nonnull(), ho = mo.nonnull(), hie = ie.nonnull(), hde = de.nonnull();
   if (!hx && !ho && !hie && !hde) {
     // null step: no wavefront; the extension finds no M (wavefront_extend_end2end)
     if (G > 1) g.sync();
     d.num_null = nn + 1;
-    set_desc(c, s, 0, kAbsent, INT_MIN, 0, 0);
-    set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
-    set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
+    set_desc<MODE>(c, s, 0, kAbsent, INT_MIN, 0, 0);
+    set_desc<MODE>(c, s, 1, kAbsent, INT_MIN, 0, 0);
+    set_desc<MODE>(c, s, 2, kAbsent, INT_MIN, 0, 0);
     if (nn + 1 > c.scope) { d.status = ST_END_UNREACHABLE; d.status_score = s; return 1; }
     return 0;
   }
@@ -316,7 +323,7 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   const int width = hi - lo + 1;
   WfRef om, oi, od;
   int offm = 0, offi = 0, offd = 0, need = 0;
-  if (!c.leaf) {
+  if (!kLeaf) {
     if (width > c.W) return -1;
     om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
     oi.base = om.base + c.W;
@@ -382,13 +389,13 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   g.minmax(r, mm);
   g.sync();
   d.num_null = 0;
-  if (c.leaf) d.lused = used + need;
+  if (kLeaf) d.lused = used + need;
   else { c.rphys[slot_of(c, s)] = nphys; d.next_phys = (nphys + 1 == c.nphys) ? 0 : nphys + 1; }
-  if (r[0] <= r[1]) set_desc(c, s, 0, r[0], r[1], offm, lo); else set_desc(c, s, 0, lo, lo - 1, offm, lo);
-  if (ai) { if (r[2] <= r[3]) set_desc(c, s, 1, r[2], r[3], offi, lo); else set_desc(c, s, 1, lo, lo - 1, offi, lo); }
-  else set_desc(c, s, 1, kAbsent, INT_MIN, 0, 0);
-  if (ad) { if (r[4] <= r[5]) set_desc(c, s, 2, r[4], r[5], offd, lo); else set_desc(c, s, 2, lo, lo - 1, offd, lo); }
-  else set_desc(c, s, 2, kAbsent, INT_MIN, 0, 0);
+  if (r[0] <= r[1]) set_desc<MODE>(c, s, 0, r[0], r[1], offm, lo); else set_desc<MODE>(c, s, 0, lo, lo - 1, offm, lo);
+  if (ai) { if (r[2] <= r[3]) set_desc<MODE>(c, s, 1, r[2], r[3], offi, lo); else set_desc<MODE>(c, s, 1, lo, lo - 1, offi, lo); }
+  else set_desc<MODE>(c, s, 1, kAbsent, INT_MIN, 0, 0);
+  if (ad) { if (r[4] <= r[5]) set_desc<MODE>(c, s, 2, r[4], r[5], offd, lo); else set_desc<MODE>(c, s, 2, lo, lo - 1, offd, lo); }
+  else set_desc<MODE>(c, s, 2, kAbsent, INT_MIN, 0, 0);
   // wavefront_termination_end2end on component_end at score s
   const int ak = sv.tlen - sv.plen;
   bool done;
@@ -462,20 +469,20 @@ __device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s
                                      const Grp<G> g) {
   const DirCfg c0 = d0.cfg, c1 = d1.cfg;
   const int plen = d0.sv.plen, tlen = d0.sv.tlen;
-  const WfRef m0 = ref_raw(c0, s0, 0);
+  const WfRef m0 = ref_raw<0>(c0, s0, 0);
   if (!m0.present()) return;
-  const WfRef dd0 = ref_raw(c0, s0, 2);
-  const WfRef ii0 = ref_raw(c0, s0, 1);
+  const WfRef dd0 = ref_raw<0>(c0, s0, 2);
+  const WfRef ii0 = ref_raw<0>(c0, s0, 1);
   for (int i = 0; i < p.scope; ++i) {
     const int si = s1 - i;
     if (si < 0) break;
     if (s0 + si - p.o >= bp.score) continue;
-    const WfRef dd1 = ref_raw(c1, si, 2);
+    const WfRef dd1 = ref_raw<0>(c1, si, 2);
     if (dd0.present() && dd1.present()) bp_scan<G>(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, g);
-    const WfRef ii1 = ref_raw(c1, si, 1);
+    const WfRef ii1 = ref_raw<0>(c1, si, 1);
     if (ii0.present() && ii1.present()) bp_scan<G>(false, fwd, s0, si, ii0, ii1, plen, tlen, p.o, CI, bp, g);
     if (s0 + si >= bp.score) continue;
-    const WfRef mm1 = ref_raw(c1, si, 0);
+    const WfRef mm1 = ref_raw<0>(c1, si, 0);
     if (mm1.present()) bp_scan<G>(true, fwd, s0, si, m0, mm1, plen, tlen, p.o, CM, bp, g);
   }
 }
@@ -521,14 +528,14 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
   for (;;) {
     if (fmax + rmax >= max_antidiag) break;
     ++sf;
-    const int qf = dir_step<G>(F, p, sf, g, &ak);
+    const int qf = dir_step<G, 0>(F, p, sf, g, &ak);
     if (qf < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (fmax < ak) fmax = ak;
     last_fwd = true;
     if (qf) return F.status;
     if (fmax + rmax >= max_antidiag) break;
     ++sr;
-    const int qr = dir_step<G>(R, p, sr, g, &ak);
+    const int qr = dir_step<G, 0>(R, p, sr, g, &ak);
     if (qr < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (rmax < ak) rmax = ak;
     last_fwd = false;
@@ -542,7 +549,7 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
       if (sf + min_sr - p.o >= bp.score) break;
       overlap<G>(F, R, sf, sr, true, bp, p, g);
       ++sr;
-      const int q = dir_step<G>(R, p, sr, g, &ak);
+      const int q = dir_step<G, 0>(R, p, sr, g, &ak);
       if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
       if (q) return R.status;
     }
@@ -550,7 +557,7 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
     if (min_sf + sr - p.o >= bp.score) break;
     overlap<G>(R, F, sr, sf, false, bp, p, g);
     ++sf;
-    const int q = dir_step<G>(F, p, sf, g, &ak);
+    const int q = dir_step<G, 0>(F, p, sf, g, &ak);
     if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (q) return F.status;
     if (sr + sf >= max_steps) return WFG_ST_MAX_STEPS;
@@ -585,7 +592,7 @@ struct RunOut {
 // unshifted null when the source is absent or out of range.
 __device__ __forceinline__ long long bt_src(const DirCfg& B, int score, int ci, int kk, int add, int type) {
   if (score < 0) return (long long)kNull;
-  const WfRef w = ref_raw(B, score, ci);
+  const WfRef w = ref_raw<1>(B, score, ci);
   if (w.lo <= kk && kk <= w.hi) return (long long)(w.at(kk) + add) * 16LL + type;
   return (long long)kNull;
 }
@@ -606,7 +613,7 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
       // wavefront_unialign_reached_limits checks the step count after compute, before extend
       if (s >= max_steps) return WFG_ST_UNATTAINABLE;
       if (s > guard) return WFG_ST_UNATTAINABLE;
-      const int q = dir_step<G>(B, p, s, g, &ak);
+      const int q = dir_step<G, 1>(B, p, s, g, &ak);
       if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
       if (q) break;
     }
@@ -961,6 +968,31 @@ int biwfa_warps_per_block() { return 4; }
 
 cudaError_t biwfa_occupancy(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<1, 4, false, kMinBlocksPerSM>,
+                                                       4 * 32, 0);
+}
+
+// Resident blocks per SM of a shape (dyn: its dynamic shared memory in bytes).
+cudaError_t biwfa_occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm) {
+  if (gw <= 1) return biwfa_occupancy(blocks_per_sm);
+  if (gw == 8) {
+    if (ring_in_smem) {
+      const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<8, 1, true, 1>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+      if (e != cudaSuccess) return e;
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<8, 1, true, 1>,
+                                                           8 * 32, dyn);
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<8, 1, false, 2>,
+                                                         8 * 32, 0);
+  }
+  if (ring_in_smem) {
+    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<4, 1, true, 1>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<4, 1, true, 1>,
+                                                         4 * 32, dyn);
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<4, 1, false, 3>,
                                                        4 * 32, 0);
 }
 

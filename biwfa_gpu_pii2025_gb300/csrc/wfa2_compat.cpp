@@ -172,7 +172,7 @@ int wavefront_align_batch(wavefront_aligner_t* const wf, const int n, const char
   im->runs.resize((size_t)std::max<int64_t>(total + n, 1));
   const wfg_config_t cfg = config_of(im);
   int64_t nruns = 0;
-  const int st = wfg_align_host(im->ctx, &cfg, WFG_SCHED_PLAIN, n, im->seq.data(), total, im->p_off.data(),
+  const int st = wfg_align_host(im->ctx, &cfg, WFG_SCHED_SORTED, n, im->seq.data(), total, im->p_off.data(),
                                 im->plen.data(), im->t_off.data(), im->tlen.data(), im->scores.data(),
                                 im->statuses.data(), im->run_off.data(), im->run_len.data(), im->runs.data(),
                                 (int64_t)im->runs.size(), &nruns);

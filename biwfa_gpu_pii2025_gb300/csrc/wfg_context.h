@@ -65,6 +65,7 @@ constexpr int kNumCounters = kOutHeadIndex + 4;
 // Kernel launchers (biwfa_kernel.cu, mlp_kernel.cu).
 cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream);
 cudaError_t biwfa_occupancy(int* blocks_per_sm);
+cudaError_t biwfa_occupancy_shape(int group_warps, int ring_in_smem, size_t dyn_smem, int* blocks_per_sm);
 int biwfa_warps_per_block();
 int biwfa_groups_per_block(int group_warps, int ring_in_smem);
 cudaError_t launch_pack(int n, const uint8_t* ascii, PairDesc* pairs, uint32_t* words, int num_sms,
@@ -79,6 +80,9 @@ cudaError_t launch_mlp_train_step(const void* feats_bf16, const float* target, c
                                   int num_sms, cudaStream_t stream);
 cudaError_t launch_mlp_adam(float* master, const float* grad, float* m, float* v, float lr, float beta1, float beta2,
                             float eps, const int* step, void* w1t, void* w2t, cudaStream_t stream);
+int sched_bin_words();
+cudaError_t launch_bin_order(int n, const float* pred, float wide_threshold, int wide_cap, int* work, int* stats,
+                             int* order, int num_sms, cudaStream_t stream);
 cudaError_t launch_mlp_sync_bf16(const float* master, void* w1t, void* w2t, cudaStream_t stream);
 
 }  // namespace wfg
@@ -108,6 +112,7 @@ struct wfg_context {
   wfg::DevBuf<int64_t> d_runoff;
   wfg::DevBuf<uint32_t> d_runs;
   wfg::DevBuf<unsigned long long> d_counters;
+  wfg::DevBuf<unsigned long long> d_batch_heads;  // work-queue cursors of the plain path's launches
   wfg::DevBuf<uint8_t> d_arena;
   wfg::DevBuf<uint8_t> d_flush;
   wfg::PinBuf<unsigned long long> h_counters;
@@ -120,6 +125,8 @@ struct wfg_context {
   // learned scheduling
   wfg::DevBuf<uint16_t> d_feats;   // num_pairs x 32 bf16
   wfg::DevBuf<float> d_pred;       // predicted scores
+  wfg::DevBuf<int> d_bin_work;     // device binning scratch (histogram, cursors, stats)
+  wfg::PinBuf<int> h_bin_stats;    // bin sizes and maxima read back by the learned schedule
   bool feats_valid = false;
   bool pred_valid = false;
   wfg_model* model = nullptr;
@@ -131,6 +138,7 @@ struct wfg_context {
     int wide_warps = 8;
     int wide_smem = 1;
     float ring_margin = 1.4f;       // ring width = margin * predicted score / e + 64
+    int retry_warps = 8;            // warps per pair in the retry passes (their pairs are wide)
   } tune;
   cudaStream_t aux_stream = nullptr;
   // wfg_run's device work as a CUDA graph (wfg_set_graph)

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -75,6 +76,8 @@ void wfg_context_destroy(wfg_context_t* c) {
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   c->h_order_pin.release();
+  c->d_feats.release(); c->d_pred.release(); c->d_bin_work.release(); c->h_bin_stats.release();
+  c->d_batch_heads.release();
   cudaStreamDestroy(c->stream);
   cudaStreamDestroy(c->aux_stream);
   delete c;
@@ -194,6 +197,7 @@ struct Launch {
   int smem = 0;          // rings in shared memory
   int ring_w = 0, leaf_words = 0, leaf_max_score = 0, run_cap = 0, leaf_run_cap = 0, stack_cap = 0;
   int64_t groups = 0;    // pairs in flight
+  bool batched = false;  // consecutive launches of `groups` pairs each instead of one persistent launch
   ArenaLayout L{};
   int64_t arena_off = 0; // byte offset of this launch's arenas
   int order_off = 0, count = 0;
@@ -240,13 +244,14 @@ void size_launch(const wfg_context* c, const IntPen& p, int pass, int ring_w_hin
 }
 
 // Groups that fit the device at once for a shape (persistent grid).
-int64_t max_groups(const wfg_context* c, int gw) {
-  if (gw <= 1) {
-    int bps = 0;
-    if (biwfa_occupancy(&bps) != cudaSuccess || bps < 1) bps = 1;
-    return (int64_t)bps * c->num_sms * biwfa_groups_per_block(1, 0);
+int64_t max_groups(const wfg_context* c, const IntPen& p, const Launch& l) {
+  const size_t dyn = l.smem ? (size_t)2 * p.nphys * 3 * (size_t)l.ring_w * sizeof(int32_t) : 0;
+  int bps = 0;
+  if (biwfa_occupancy_shape(l.gw, l.smem, dyn, &bps) != cudaSuccess || bps < 1) {
+    (void)cudaGetLastError();
+    bps = 1;
   }
-  return (int64_t)c->num_sms * (gw == 4 ? 2 : 1);
+  return (int64_t)bps * c->num_sms * biwfa_groups_per_block(l.gw, l.smem);
 }
 
 }  // namespace
@@ -276,65 +281,71 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   c->last_score_only = cfg->score_only;
   // ---- order and pass-0 launches
   std::vector<int> order((size_t)n);
+  bool order_on_device = false;  // the learned schedule writes the order on the device
   std::vector<Launch> first;  // concurrent pass-0 launches
   if (sched == WFG_SCHED_GIVEN && c->have_order) {
     order = c->h_order;
     Launch l; l.gw = c->force_gw; l.smem = c->force_smem; l.count = n;
     first.push_back(l);
   } else if (sched == WFG_SCHED_LEARNED && (c->have_pred || c->model != nullptr)) {
+    // Predictions on the device: the model's (4-mer features + MLP forward, recomputed every
+    // run) or the caller's. Binning and ordering also run on the device (launch_bin_order):
+    // one order by predicted score, largest first; its head — the pairs predicted at or above
+    // the wide threshold, at most one resident wave of the multi-warp shape — forms the
+    // multi-warp launch (aux stream), the rest the single-warp launch. Rings are sized from
+    // each launch's largest prediction (a mispredicted pair overflows into the retry passes).
+    // Only the two launch sizes and prediction bounds come back to the host.
+    WFG_CHECK(c, c->d_pred.reserve((size_t)std::max(n, 1)));
     if (c->model != nullptr) {
-      // Predict on the device (4-mer features + MLP), then bin on the host.
+      c->feats_valid = false;
       const int st = wfg_model_predict(c->model, c, nullptr);
       if (st != WF_STATUS_ALG_COMPLETED) return st;
-      c->h_pred.resize((size_t)n);
-      if (n > 0) {
-        WFG_CHECK(c, cudaMemcpyAsync(c->h_pred.data(), c->d_pred.ptr, sizeof(float) * (size_t)n,
-                                     cudaMemcpyDeviceToHost, c->stream));
-        WFG_CHECK(c, cudaStreamSynchronize(c->stream));
-      }
+    } else if (n > 0) {
+      WFG_CHECK(c, cudaMemcpyAsync(c->d_pred.ptr, c->h_pred.data(), sizeof(float) * (size_t)n, cudaMemcpyHostToDevice,
+                                   c->stream));
     }
-    // Wide pairs (predicted score above the threshold) go to a multi-warp launch on a second
-    // stream, the rest to the single-warp launch; each group is ordered by predicted work,
-    // largest first, and its rings are sized from its largest prediction (a mispredicted
-    // pair overflows into the retry passes).
-    const float thr = c->tune.wide_threshold;
-    std::vector<int> wide, narrow;
-    float max_wide = 0.f, max_narrow = 0.f;
-    for (int i = 0; i < n; ++i) {
-      const float s = c->h_pred[(size_t)i];
-      if (c->tune.wide_warps > 1 && s >= thr) { wide.push_back(i); max_wide = std::max(max_wide, s); }
-      else { narrow.push_back(i); max_narrow = std::max(max_narrow, s); }
+    const bool use_wide = c->tune.wide_warps > 1 && c->tune.wide_threshold < 3.0e38f;  // FLT_MAX: no wide launch
+    int64_t wide_cap = 0;
+    if (use_wide) {
+      Launch lw; lw.gw = c->tune.wide_warps; lw.smem = c->tune.wide_smem; lw.ring_w = kSmemRingW;
+      wide_cap = max_groups(c, p, lw);
     }
-    auto by_pred = [&](int a, int b) {
-      const float pa = c->h_pred[(size_t)a], pb = c->h_pred[(size_t)b];
-      if (pa != pb) return pa > pb;
-      return c->h_plen[(size_t)a] + c->h_tlen[(size_t)a] > c->h_plen[(size_t)b] + c->h_tlen[(size_t)b];
-    };
-    std::stable_sort(wide.begin(), wide.end(), by_pred);
-    std::stable_sort(narrow.begin(), narrow.end(), by_pred);
-    std::copy(wide.begin(), wide.end(), order.begin());
-    std::copy(narrow.begin(), narrow.end(), order.begin() + (ptrdiff_t)wide.size());
+    WFG_CHECK(c, c->d_bin_work.reserve((size_t)sched_bin_words()));
+    WFG_CHECK(c, c->h_bin_stats.reserve(4));
+    WFG_CHECK(c, launch_bin_order(n, c->d_pred.ptr, use_wide ? c->tune.wide_threshold : INFINITY, (int)wide_cap,
+                                  c->d_bin_work.ptr, c->d_bin_work.ptr + sched_bin_words() - 4, c->d_order.ptr,
+                                  c->num_sms, c->stream));
+    WFG_CHECK(c, cudaMemcpyAsync(c->h_bin_stats.ptr, c->d_bin_work.ptr + sched_bin_words() - 4, sizeof(int) * 4,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    WFG_CHECK(c, cudaStreamSynchronize(c->stream));
+    order_on_device = true;
+    const int n_wide = c->h_bin_stats.ptr[0], n_narrow = c->h_bin_stats.ptr[1];
+    float max_wide, max_narrow;
+    memcpy(&max_wide, &c->h_bin_stats.ptr[2], sizeof(float));
+    memcpy(&max_narrow, &c->h_bin_stats.ptr[n_wide > 0 ? 3 : 2], sizeof(float));
     const double m = c->tune.ring_margin;
-    if (!wide.empty()) {
-      Launch l; l.gw = c->tune.wide_warps; l.order_off = 0; l.count = (int)wide.size();
+    if (n_wide > 0) {
+      Launch l; l.gw = c->tune.wide_warps; l.order_off = 0; l.count = n_wide;
       const int w_need = (int)(m * max_wide / std::max(p.e, 1)) + 64;
       l.smem = (c->tune.wide_smem && next_pow2((uint64_t)w_need) <= (uint32_t)kSmemRingW) ? 1 : 0;
       l.ring_w = w_need;
       first.push_back(l);
     }
-    if (!narrow.empty()) {
-      Launch l; l.gw = 1; l.order_off = (int)wide.size(); l.count = (int)narrow.size();
+    if (n_narrow > 0) {
+      Launch l; l.gw = 1; l.order_off = n_wide; l.count = n_narrow;
       l.ring_w = (int)(m * max_narrow / std::max(p.e, 1)) + 64;
       first.push_back(l);
     }
   } else {
-    // Plain path: longest pairs first, a stable counting sort on plen + tlen (O(n)).
+    // Plain and sorted paths: longest pairs first, a stable counting sort on plen + tlen (O(n)).
+    // The plain path then runs them in consecutive launches of one resident set each.
     std::vector<int> cnt((size_t)c->max_sum + 2, 0);
     for (int i = 0; i < n; ++i) cnt[(size_t)(c->max_sum - (c->h_plen[(size_t)i] + c->h_tlen[(size_t)i])) + 1]++;
     for (size_t v = 1; v < cnt.size(); ++v) cnt[v] += cnt[v - 1];
     for (int i = 0; i < n; ++i)
       order[(size_t)cnt[(size_t)(c->max_sum - (c->h_plen[(size_t)i] + c->h_tlen[(size_t)i]))]++] = i;
     Launch l; l.gw = c->force_gw; l.smem = c->force_smem; l.count = n;
+    l.batched = (sched == WFG_SCHED_PLAIN);
     first.push_back(l);
   }
   if (first.empty()) { Launch l; l.count = 0; first.push_back(l); }
@@ -346,7 +357,7 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     if (l.gw != 1 && l.gw != 4 && l.gw != 8) l.gw = 8;
     const int hint = l.ring_w > 0 ? l.ring_w : c->limit_ring_w;
     size_launch(c, p, 0, hint, l);
-    int64_t gmax = std::min<int64_t>(max_groups(c, l.gw), std::max<int64_t>(1, l.count));
+    int64_t gmax = std::min<int64_t>(max_groups(c, p, l), std::max<int64_t>(1, l.count));
     const int64_t fit = (arena_budget / (int64_t)first.size()) / std::max<int64_t>(l.L.total, 1);
     l.groups = std::max<int64_t>(1, std::min(gmax, fit));
     const int gpb = biwfa_groups_per_block(l.gw, l.smem);
@@ -358,20 +369,25 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   int64_t arena_need = pass0_bytes;
   for (int ps = 1; ps < kNumPasses; ++ps) {
     Launch& l = retry[ps];
-    l.gw = 1;
+    l.gw = c->tune.retry_warps;  // pairs that overflowed the first pass are wide
     size_launch(c, p, ps, 0, l);
-    int64_t gmax = std::min<int64_t>(max_groups(c, 1), std::max<int64_t>(4, (int64_t)n));
-    gmax = std::min<int64_t>(gmax, ps == 1 ? (int64_t)c->num_sms * 4 : (int64_t)c->num_sms * 2);
+    const int gpb = biwfa_groups_per_block(l.gw, l.smem);
+    int64_t gmax = std::min<int64_t>(max_groups(c, p, l), std::max<int64_t>(gpb, (int64_t)n));
+    if (l.gw == 1) gmax = std::min<int64_t>(gmax, ps == 1 ? (int64_t)c->num_sms * 4 : (int64_t)c->num_sms * 2);
     const int64_t fit = arena_budget / std::max<int64_t>(l.L.total, 1);
-    l.groups = std::max<int64_t>(4, (std::min(gmax, fit) / 4) * 4);
+    l.groups = std::max<int64_t>(gpb, (std::min(gmax, fit) / gpb) * gpb);
     arena_need = std::max(arena_need, l.groups * l.L.total);
   }
   WFG_CHECK(c, c->d_arena.reserve((size_t)arena_need));
+  int64_t num_batches = 0;
+  for (const Launch& l : first)
+    if (l.batched) num_batches += (l.count + l.groups - 1) / l.groups;
+  WFG_CHECK(c, c->d_batch_heads.reserve((size_t)std::max<int64_t>(num_batches, 1)));
   // The order goes through a pinned buffer (a graph's copy node reads it when the graph
   // runs): wait until the previous run's copy of it is done before overwriting it.
   if (c->ran) WFG_CHECK(c, cudaEventSynchronize(c->ev[0]));
   WFG_CHECK(c, c->h_order_pin.reserve((size_t)std::max(n, 1)));
-  if (n > 0) std::copy(order.begin(), order.end(), c->h_order_pin.ptr);
+  if (n > 0 && !order_on_device) std::copy(order.begin(), order.end(), c->h_order_pin.ptr);
   auto params = [&](const Launch& l, int ps) {
     KernelParams kp{};
     kp.x = p.x; kp.o = p.o; kp.e = p.e; kp.scope = p.scope;
@@ -412,18 +428,39 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     };
     cudaError_t e = cudaSuccess;
     launches = 1;
-    if (n > 0 && (e = cudaMemcpyAsync(c->d_order.ptr, c->h_order_pin.ptr, sizeof(int) * (size_t)n,
-                                      cudaMemcpyHostToDevice, c->stream)) != cudaSuccess) return e;
+    if (n > 0 && !order_on_device &&
+        (e = cudaMemcpyAsync(c->d_order.ptr, c->h_order_pin.ptr, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice,
+                             c->stream)) != cudaSuccess)
+      return e;
     if ((e = mark(c->ev[0])) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(c->d_counters.ptr, 0, sizeof(unsigned long long) * kNumCounters, c->stream)) != cudaSuccess)
+      return e;
+    if (num_batches > 0 && (e = cudaMemsetAsync(c->d_batch_heads.ptr, 0, sizeof(unsigned long long) * (size_t)num_batches,
+                                                c->stream)) != cudaSuccess)
       return e;
     if ((e = launch_pack(n, c->d_seq.ptr, c->d_pairs.ptr, c->d_words.ptr, c->num_sms, c->stream)) != cudaSuccess) return e;
     if ((e = mark(c->ev[1])) != cudaSuccess) return e;
     // pass 0: the first launch on the context's stream, a second one (wide pairs) on the aux
     // stream, joined before the retry passes
+    int64_t batch_index = 0;
     for (size_t li = 0; li < first.size(); ++li) {
       const Launch& l = first[li];
       if (l.count <= 0) continue;
+      if (l.batched) {
+        // one launch per resident set of pairs, each waiting for its slowest pair
+        const int gpb = biwfa_groups_per_block(l.gw, l.smem);
+        for (int64_t b0 = 0; b0 < l.count; b0 += l.groups, ++batch_index) {
+          KernelParams kp = params(l, 0);
+          kp.num_pairs = (int)std::min<int64_t>(l.groups, l.count - b0);
+          kp.num_pairs_ptr = nullptr;
+          kp.order = c->d_order.ptr + l.order_off + b0;
+          kp.queue_head = c->d_batch_heads.ptr + batch_index;
+          const int blocks = (int)((kp.num_pairs + gpb - 1) / gpb);
+          if ((e = launch_biwfa(kp, blocks, c->stream)) != cudaSuccess) return e;
+          ++launches;
+        }
+        continue;
+      }
       KernelParams kp = params(l, 0);
       kp.num_pairs = l.count;
       kp.num_pairs_ptr = nullptr;
@@ -451,7 +488,8 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
       kp.num_pairs_ptr = c->d_counters.ptr + (ps - 1) * kCountersPerPass + 1;
       kp.order = c->d_retry.ptr + (size_t)(ps - 1) * n;
       kp.queue_head = c->d_counters.ptr + ps * kCountersPerPass + 0;
-      if ((e = launch_biwfa(kp, (int)(l.groups / 4), c->stream)) != cudaSuccess) return e;
+      if ((e = launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), c->stream)) != cudaSuccess)
+        return e;
       ++launches;
     }
     if ((e = mark(c->ev[3])) != cudaSuccess) return e;
@@ -490,6 +528,12 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   c->stats.ring_w = first[0].ring_w;
   c->stats.arena_bytes = first[0].L.total;
   c->ran = true;
+  return WF_STATUS_ALG_COMPLETED;
+}
+
+int wfg_set_retry_shape(wfg_context_t* c, int group_warps) {
+  if (!c || (group_warps != 1 && group_warps != 4 && group_warps != 8)) return WF_STATUS_UNSUPPORTED;
+  c->tune.retry_warps = group_warps;
   return WF_STATUS_ALG_COMPLETED;
 }
 

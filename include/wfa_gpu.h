@@ -220,9 +220,15 @@ typedef struct {
 
 /* Scheduling policy of wfg_run. */
 typedef enum {
-  WFG_SCHED_PLAIN = 0,    /* pairs sorted by length (descending), one arena size for all */
-  WFG_SCHED_LEARNED = 1,  /* pairs binned and ordered by the score predictor's output */
-  WFG_SCHED_GIVEN = 2,    /* the caller's order (wfg_set_order) */
+  /* pairs sorted by length (descending) and aligned in consecutive launches of as many
+   * pairs as the GPU holds at once (one warp per pair); each launch ends with its slowest
+   * pair (the plain batched GPU path) */
+  WFG_SCHED_PLAIN = 0,
+  /* pairs binned and ordered by the score predictor's output, one persistent work-stealing
+   * launch per bin, scratch sized from the prediction */
+  WFG_SCHED_LEARNED = 1,
+  WFG_SCHED_GIVEN = 2,    /* the caller's order (wfg_set_order), one persistent launch */
+  WFG_SCHED_SORTED = 3,   /* pairs sorted by length (descending), one persistent launch */
 } wfg_sched_t;
 
 typedef struct {
@@ -281,6 +287,9 @@ int wfg_set_exec_shape(wfg_context_t* ctx, int group_warps, int ring_in_smem);
  * instantiated graph with cudaGraphExecUpdate when the topology is unchanged. enable = 0
  * issues the same work directly on the streams. Default 1. */
 int wfg_set_graph(wfg_context_t* ctx, int enable);
+/* Warps per pair (1, 4 or 8, HBM rings) of the two retry passes, which realign the pairs that
+ * overflowed the first pass's scratch: those are the widest pairs. Default 8. */
+int wfg_set_retry_shape(wfg_context_t* ctx, int group_warps);
 /* Policy of WFG_SCHED_LEARNED: pairs whose predicted score is at least wide_threshold run
  * with wide_warps warps per pair (rings in shared memory when wide_smem and they fit),
  * concurrently with the single-warp launch for the rest; ring widths are

@@ -72,16 +72,20 @@ def test_gpu_score_only_matches_oracle(batch_aligner):
         assert res.scores[i] == binding.oracle_align(b.pattern(i), b.text(i), score_only=True)[1]
 
 
-def test_overflow_retry_passes_keep_results_exact(batch_aligner):
-    """Tiny first-pass arenas push most pairs into the retry passes; results must not move."""
+@pytest.mark.parametrize("retry_warps", [8, 4, 1])
+def test_overflow_retry_passes_keep_results_exact(batch_aligner, retry_warps):
+    """Tiny first-pass arenas push most pairs into the retry passes (of each shape); results
+    must not move."""
     b = pkg.PairBatch.generate(5, 200, seed=31)
     ref = batch_aligner.align(b)
     try:
         batch_aligner.set_arena_limits(ring_w=16, leaf_words=64)
+        batch_aligner.set_retry_shape(retry_warps)
         res = batch_aligner.align(b)
         st = batch_aligner.stats()
     finally:
         batch_aligner.set_arena_limits(0, 0)
+        batch_aligner.set_retry_shape(8)
     assert st.retried_pairs > 0
     assert (res.status == 0).all()
     assert np.array_equal(res.scores, ref.scores)
