@@ -282,6 +282,7 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   // ---- order and pass-0 launches
   std::vector<int> order((size_t)n);
   bool order_on_device = false;  // the learned schedule writes the order on the device
+  int predict_launches = 0;      // features, MLP forward and binning kernels of the learned schedule
   std::vector<Launch> first;  // concurrent pass-0 launches
   if (sched == WFG_SCHED_GIVEN && c->have_order) {
     order = c->h_order;
@@ -319,6 +320,7 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
                                  cudaMemcpyDeviceToHost, c->stream));
     WFG_CHECK(c, cudaStreamSynchronize(c->stream));
     order_on_device = true;
+    predict_launches = (c->model != nullptr ? 2 : 0) + (n > 0 ? 3 : 0);
     const int n_wide = c->h_bin_stats.ptr[0], n_narrow = c->h_bin_stats.ptr[1];
     float max_wide, max_narrow;
     memcpy(&max_wide, &c->h_bin_stats.ptr[2], sizeof(float));
@@ -523,7 +525,7 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   } else {
     WFG_CHECK(c, enqueue(false));
   }
-  c->stats.launches = launches;
+  c->stats.launches = launches + predict_launches;
   c->stats.num_warps = (int)(first[0].groups * first[0].gw);
   c->stats.ring_w = first[0].ring_w;
   c->stats.arena_bytes = first[0].L.total;

@@ -235,7 +235,8 @@ typedef struct {
   double kernel_ms;       /* device time of the alignment kernels of the last wfg_run */
   double pack_ms;         /* device time of the packing kernel */
   double total_ms;        /* device time of the whole wfg_run (events on the context's stream) */
-  int launches;           /* kernels this library launched in the last wfg_run */
+  int launches;           /* kernels this library launched in the last wfg_run (packing, alignment
+                             passes, and the learned schedule's feature, MLP and binning kernels) */
   int retried_pairs;      /* pairs rerun with a larger arena after a scratch overflow */
   int num_warps;          /* resident warps of the main launch */
   int ring_w;             /* ring width (diagonals) of the main launch */
