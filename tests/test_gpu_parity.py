@@ -233,7 +233,8 @@ def _check_properties(b, res, penalties=(0, 4, 6, 2)):
     assert not same.any()
 
 
-@pytest.mark.parametrize("workload,n,sample", [(1, 10_000, 10_000), (2, 1_000_000, 20_000), (3, 200_000, 2_000)])
+@pytest.mark.parametrize("workload,n,sample", [(1, 10_000, 10_000), (2, 1_000_000, 20_000), (3, 200_000, 2_000),
+                                               (4, 2_000, 16), (5, 1_000_000, 5_000)])
 def test_full_size_workloads(batch_aligner, workload, n, sample):
     """Full-size workloads: every pair checked by properties; a seeded sample bit-exact vs the oracle."""
     b = pkg.PairBatch.generate(workload, n, seed=5000 + workload)
