@@ -31,10 +31,14 @@ constexpr int kMaxScope = 32;
 #define WFG_G1_MIN_BLOCKS 6
 #endif
 #ifndef WFG_STEP_UNROLL
-#define WFG_STEP_UNROLL 2
+#define WFG_STEP_UNROLL 3
 #endif
 constexpr int kMinBlocksPerSM = WFG_G1_MIN_BLOCKS;  // 6: caps registers so 24 warps fit on an SM
-constexpr int kStepUnroll = WFG_STEP_UNROLL;        // diagonals per thread per step iteration
+#ifndef WFG_LEAF_UNROLL
+#define WFG_LEAF_UNROLL 2
+#endif
+constexpr int kStepUnroll = WFG_STEP_UNROLL;        // diagonals per thread per step iteration (rings)
+constexpr int kLeafUnroll = WFG_LEAF_UNROLL;        // the same for the leaf store (narrower steps)
 constexpr int ST_OK = -1, ST_END_REACHED = -2, ST_END_UNREACHABLE = -3;
 constexpr int CM = 0, CI = 1, CD = 3;      // components (affine2p_matrix_type values)
 constexpr int kFallbackMinScore = 250, kFallbackMinLength = 100, kRecoveryMinScore = 500;
@@ -135,7 +139,7 @@ struct Grp {
     if (G == 1) __syncwarp();
     else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(G * 32) : "memory");
   }
-  // min/max of up to 6 values at once (slot j of each warp in red[warp*8 + j])
+  // min/max of up to 8 values at once (slot j of each warp in red[warp*8 + j])
   template <int N>
   __device__ __forceinline__ void minmax(int (&v)[N], const bool (&is_max)[N]) const {
     #pragma unroll
@@ -345,7 +349,7 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   // U diagonals per thread per iteration, so that their loads are in flight together. For
   // k > hi every input read falls outside its input's [lo, hi] (the output range covers
   // them), so those lanes read nothing and store nothing.
-  constexpr int U = kStepUnroll;
+  constexpr int U = kLeaf ? kLeafUnroll : kStepUnroll;
   for (int kb = lo + g.tid; kb <= hi; kb += U * 32 * G) {
     int32_t mv[U], iv[U], dv[U];
     uint32_t xw[U];

@@ -1,6 +1,8 @@
 """Learned scheduling on the GPU: features and gradients against the float64 CPU oracle
 (oracle/mlp_oracle.py), training on plain-method scores, and results that never depend on
 the model."""
+import time
+
 import numpy as np
 import pytest
 
@@ -77,4 +79,49 @@ def test_training_learns_scores_and_schedule_keeps_results(aligner):
         for i in range(test.n):
             assert np.array_equal(got.runs_of(i), ref.runs_of(i))
     finally:
+        pred.close()
+
+
+def test_trained_network_gains_over_the_method_without_it(aligner):
+    """What the trained network adds: (1) it ranks pairs by alignment cost better than pair
+    length (the plain path's only signal), since error rates vary 10x at equal length; (2) the
+    learned-binned persistent schedule aligns a mixture batch faster than the plain length-
+    sorted batched path, with identical results (the speed-up is measured, with a wide margin
+    so that it holds on any GB300)."""
+    train = pkg.PairBatch.generate(5, 20000, seed=9101)
+    res = aligner.align(train, score_only=True)
+    pred = pkg.ScorePredictor(aligner, seed=5)
+    try:
+        pred.train(-res.scores, epochs=20, batch_rows=1024, lr=3e-3)
+        test = pkg.PairBatch.generate(5, 60000, seed=9102)
+        ref = aligner.align(test, sched=_capi.SCHED_PLAIN)
+        aligner.upload(test)
+        p = pred.predict()
+        cost = -ref.scores.astype(np.float64)
+        rank = lambda v: np.argsort(np.argsort(v, kind="stable"), kind="stable")
+        corr_net = np.corrcoef(rank(p), rank(cost))[0, 1]
+        corr_len = np.corrcoef(rank(test.plen + test.tlen), rank(cost))[0, 1]
+        assert corr_net > corr_len + 0.02, (corr_net, corr_len)
+        # among pairs of similar length, only the network separates cheap from costly ones
+        heavy = test.plen > 3000
+        c_net = np.corrcoef(rank(p[heavy]), rank(cost[heavy]))[0, 1]
+        c_len = np.corrcoef(rank((test.plen + test.tlen)[heavy]), rank(cost[heavy]))[0, 1]
+        assert c_net > c_len + 0.1, (c_net, c_len)
+        pred.attach()
+        times = {}
+        for sched in (_capi.SCHED_PLAIN, _capi.SCHED_LEARNED):
+            best = None
+            for _ in range(3):
+                aligner.synchronize()
+                t0 = time.perf_counter()
+                aligner.run(sched=sched)  # learned: features, MLP, binning and alignment
+                aligner.synchronize()
+                ms = 1e3 * (time.perf_counter() - t0)
+                best = ms if best is None else min(best, ms)
+            times[sched] = best
+            got = aligner.fetch()
+            assert np.array_equal(got.scores, ref.scores) and np.array_equal(got.status, ref.status)
+        assert times[_capi.SCHED_LEARNED] < 0.8 * times[_capi.SCHED_PLAIN], times
+    finally:
+        aligner.lib.wfg_set_model(aligner.ctx, None)
         pred.close()
