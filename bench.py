@@ -349,7 +349,7 @@ def run_ours(args):
     out = pkg.BatchResult(pin.empty(n, np.int32), pin.empty(n, np.int32), pin.empty(n, np.int64),
                           pin.empty(n, np.int32), pin.empty(runs_cap, np.uint32))
     al.align_into(hb, out, PENALTIES, sched=sched)  # warm
-    e2e_ms, h2d, d2h = [], 0, 0
+    e2e_ms, h2d, d2h, parts = [], 0, 0, []
     for _ in range(max(1, min(args.steps, 3))):
         al.flush_l2(L2_FLUSH_BYTES)
         al.synchronize()
@@ -358,6 +358,7 @@ def run_ours(args):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
         st = al.stats()
         h2d, d2h = st.h2d_bytes, st.d2h_bytes
+        parts.append((st.upload_host_ms, st.upload_copy_ms, st.total_ms))
     e2e_t = dist.max(statistics.mean(e2e_ms))
     e2e_ok = bool(np.array_equal(out.scores[:n], res.scores)) and nruns == total_runs
     pin.close()
@@ -376,7 +377,10 @@ def run_ours(args):
             "results_identical_to_plain": same_as_plain,
             "learned": learn_info,
             "e2e": {"value": dist.sum(float(n)) / (e2e_t / 1e3), "unit": "pairs/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t, "matches_device_run": e2e_ok},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t, "matches_device_run": e2e_ok,
+                    "upload_host_ms": statistics.mean(p[0] for p in parts),
+                    "h2d_copy_ms": statistics.mean(p[1] for p in parts),
+                    "device_ms": statistics.mean(p[2] for p in parts)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": (traffic_pp * n) if traffic_pp else None,

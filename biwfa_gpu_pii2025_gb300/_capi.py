@@ -101,7 +101,8 @@ class Stats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("pack_ms", C.c_double), ("total_ms", C.c_double),
                 ("launches", C.c_int), ("retried_pairs", C.c_int), ("num_warps", C.c_int), ("ring_w", C.c_int),
                 ("arena_bytes", C.c_int64), ("total_runs", C.c_int64), ("h2d_bytes", C.c_int64),
-                ("d2h_bytes", C.c_int64), ("used_graph", C.c_int)]
+                ("d2h_bytes", C.c_int64), ("used_graph", C.c_int), ("upload_host_ms", C.c_double),
+                ("upload_copy_ms", C.c_double)]
 
 
 P = C.POINTER

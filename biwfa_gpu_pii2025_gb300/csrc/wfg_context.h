@@ -134,7 +134,8 @@ struct wfg_context {
   int force_gw = 1, force_smem = 0;
   // learned-schedule policy (wfg_set_learned_policy)
   struct {
-    float wide_threshold = 1200.f;  // predicted score from which a pair takes the wide shape
+    float wide_threshold = 1200.f;  // predicted score from which a pair may take the wide shape
+                                    // (the heaviest ones, at most one resident wave; FLT_MAX: none)
     int wide_warps = 8;
     int wide_smem = 1;
     float ring_margin = 1.4f;       // ring width = margin * predicted score / e + 64
@@ -143,6 +144,9 @@ struct wfg_context {
   cudaStream_t aux_stream = nullptr;
   // wfg_run's device work as a CUDA graph (wfg_set_graph)
   int use_graph = 1;
+  // timing of the last upload (wfg_get_stats)
+  double upload_host_ms = 0.0;
+  bool uploaded = false;
   cudaGraphExec_t graph_exec = nullptr;
   wfg::PinBuf<int> h_order_pin;  // the processing order, copied by the graph's first node
 };

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -89,6 +90,7 @@ int wfg_upload(wfg_context_t* c, int n, const char* seq, int64_t seq_len, const 
                const int* plen, const int64_t* t_off, const int* tlen) {
   if (!c || n < 0 || (n > 0 && (!seq || !p_off || !plen || !t_off || !tlen))) return WF_STATUS_UNSUPPORTED;
   cudaSetDevice(c->device);
+  const auto host_t0 = std::chrono::steady_clock::now();
   c->n = n;
   c->seq_len = seq_len;
   c->h_plen.assign(plen, plen + n);
@@ -135,8 +137,12 @@ int wfg_upload(wfg_context_t* c, int n, const char* seq, int64_t seq_len, const 
   WFG_CHECK(c, c->d_runlen.reserve((size_t)std::max(n, 1)));
   WFG_CHECK(c, c->d_runoff.reserve((size_t)std::max(n, 1)));
   WFG_CHECK(c, c->d_runs.reserve((size_t)std::max<int64_t>(out_cap, 1)));
+  c->upload_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+  WFG_CHECK(c, cudaEventRecord(c->ev[6], c->stream));
   if (seq_len > 0) WFG_CHECK(c, cudaMemcpyAsync(c->d_seq.ptr, seq, (size_t)seq_len, cudaMemcpyHostToDevice, c->stream));
   if (n > 0) WFG_CHECK(c, cudaMemcpyAsync(c->d_pairs.ptr, hp, sizeof(PairDesc) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  WFG_CHECK(c, cudaEventRecord(c->ev[7], c->stream));
+  c->uploaded = true;
   c->stats.h2d_bytes = seq_len + (int64_t)sizeof(PairDesc) * n;
   c->ran = false;
   return WF_STATUS_ALG_COMPLETED;
@@ -577,6 +583,11 @@ int wfg_get_stats(wfg_context_t* c, wfg_stats_t* out) {
     if (cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]) == cudaSuccess) c->stats.total_ms = ms;
     c->stats.retried_pairs = (int)c->h_counters.ptr[1];
     c->stats.total_runs = (int64_t)c->h_counters.ptr[kOutHeadIndex];
+  }
+  c->stats.upload_host_ms = c->upload_host_ms;
+  if (c->uploaded) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]) == cudaSuccess) c->stats.upload_copy_ms = ms;
   }
   *out = c->stats;
   return WF_STATUS_ALG_COMPLETED;

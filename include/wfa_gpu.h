@@ -244,6 +244,8 @@ typedef struct {
   int64_t total_runs;     /* CIGAR runs produced */
   int64_t h2d_bytes, d2h_bytes; /* bytes copied by the last upload / fetch */
   int used_graph;         /* 1 when the last wfg_run's device work ran as one CUDA graph */
+  double upload_host_ms;  /* host time of the last wfg_upload before its copies (validation, descriptors) */
+  double upload_copy_ms;  /* device time of the last wfg_upload's host-to-device copies */
 } wfg_stats_t;
 
 wfg_context_t* wfg_context_create(int device);
@@ -291,10 +293,11 @@ int wfg_set_graph(wfg_context_t* ctx, int enable);
 /* Warps per pair (1, 4 or 8, HBM rings) of the two retry passes, which realign the pairs that
  * overflowed the first pass's scratch: those are the widest pairs. Default 8. */
 int wfg_set_retry_shape(wfg_context_t* ctx, int group_warps);
-/* Policy of WFG_SCHED_LEARNED: pairs whose predicted score is at least wide_threshold run
- * with wide_warps warps per pair (rings in shared memory when wide_smem and they fit),
- * concurrently with the single-warp launch for the rest; ring widths are
- * ring_margin * predicted score / gap_extension + 64 diagonals. */
+/* Policy of WFG_SCHED_LEARNED: the pairs with the highest predicted scores, from
+ * wide_threshold up and at most one resident wave of the shape, run with wide_warps warps per
+ * pair (rings in shared memory when wide_smem and they fit), concurrently with the
+ * single-warp launch for the rest (wide_threshold = FLT_MAX: no multi-warp launch); ring
+ * widths are ring_margin * the launch's largest predicted score / gap_extension + 64. */
 int wfg_set_learned_policy(wfg_context_t* ctx, float wide_threshold, int wide_warps, int wide_smem,
                            float ring_margin);
 /* Autotuner for WFG_SCHED_LEARNED (requires an attached model): runs the resident batch
