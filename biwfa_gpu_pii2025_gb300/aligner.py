@@ -224,7 +224,7 @@ class BatchAligner:
         return BatchResult(scores, status, run_off, run_len, runs[:total.value])
 
     def align_into(self, b: PairBatch, out: BatchResult, penalties=(0, 4, 6, 2), score_only=False,
-                   sched=_capi.SCHED_PLAIN) -> int:
+                   sched=_capi.SCHED_SORTED) -> int:
         """End to end through wfg_align_host into caller-owned (e.g. pinned) output arrays.
         Returns the number of CIGAR runs written to out.runs."""
         cfg = self.config(penalties, score_only, 0)

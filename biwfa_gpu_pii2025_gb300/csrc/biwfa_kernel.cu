@@ -28,12 +28,12 @@ constexpr int kAbsent = INT32_MAX;         // lo of a wavefront that does not ex
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxScope = 32;
 #ifndef WFG_G1_MIN_BLOCKS
-#define WFG_G1_MIN_BLOCKS 6
+#define WFG_G1_MIN_BLOCKS 7
 #endif
 #ifndef WFG_STEP_UNROLL
-#define WFG_STEP_UNROLL 3
+#define WFG_STEP_UNROLL 2
 #endif
-constexpr int kMinBlocksPerSM = WFG_G1_MIN_BLOCKS;  // 6: caps registers so 24 warps fit on an SM
+constexpr int kMinBlocksPerSM = WFG_G1_MIN_BLOCKS;  // 7: caps registers at 72 so 28 warps fit on an SM
 #ifndef WFG_LEAF_UNROLL
 #define WFG_LEAF_UNROLL 2
 #endif
