@@ -157,9 +157,10 @@ class BatchAligner:
             raise RuntimeError(f"{what} failed ({st}): {msg}")
 
     @staticmethod
-    def config(penalties=(0, 4, 6, 2), score_only=False, max_steps=0) -> _capi.Config:
+    def config(penalties=(0, 4, 6, 2), score_only=False, max_steps=0, metric=0) -> _capi.Config:
+        """metric: _capi.METRIC_GAP_AFFINE (default), METRIC_EDIT or METRIC_INDEL (penalties unused)."""
         m, x, o, e = penalties
-        return _capi.Config(m, x, o, e, 1 if score_only else 0, max_steps)
+        return _capi.Config(m, x, o, e, 1 if score_only else 0, max_steps, metric)
 
     def upload(self, b: PairBatch):
         self._batch = b  # keep host buffers alive
@@ -205,8 +206,8 @@ class BatchAligner:
         self._check(self.lib.wfg_set_predictions(self.ctx, pred.ctypes.data_as(C.POINTER(C.c_float))),
                     "wfg_set_predictions")
 
-    def run(self, penalties=(0, 4, 6, 2), score_only=False, sched=_capi.SCHED_SORTED, max_steps=0):
-        cfg = self.config(penalties, score_only, max_steps)
+    def run(self, penalties=(0, 4, 6, 2), score_only=False, sched=_capi.SCHED_SORTED, max_steps=0, metric=0):
+        cfg = self.config(penalties, score_only, max_steps, metric)
         self._check(self.lib.wfg_run(self.ctx, C.byref(cfg), sched), "wfg_run")
 
     def fetch(self, runs_cap: int | None = None) -> BatchResult:
@@ -224,10 +225,10 @@ class BatchAligner:
         return BatchResult(scores, status, run_off, run_len, runs[:total.value])
 
     def align_into(self, b: PairBatch, out: BatchResult, penalties=(0, 4, 6, 2), score_only=False,
-                   sched=_capi.SCHED_SORTED) -> int:
+                   sched=_capi.SCHED_SORTED, metric=0) -> int:
         """End to end through wfg_align_host into caller-owned (e.g. pinned) output arrays.
         Returns the number of CIGAR runs written to out.runs."""
-        cfg = self.config(penalties, score_only, 0)
+        cfg = self.config(penalties, score_only, 0, metric)
         total = C.c_int64(0)
         st = self.lib.wfg_align_host(
             self.ctx, C.byref(cfg), sched, b.n, b.seq.ctypes.data_as(C.c_void_p), int(b.seq.shape[0]),
@@ -239,9 +240,9 @@ class BatchAligner:
         return int(total.value)
 
     def align(self, b: PairBatch, penalties=(0, 4, 6, 2), score_only=False, sched=_capi.SCHED_SORTED,
-              max_steps=0) -> BatchResult:
+              max_steps=0, metric=0) -> BatchResult:
         self.upload(b)
-        self.run(penalties, score_only, sched, max_steps)
+        self.run(penalties, score_only, sched, max_steps, metric)
         return self.fetch()
 
     def synchronize(self):

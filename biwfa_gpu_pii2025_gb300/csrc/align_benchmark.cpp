@@ -7,9 +7,10 @@
 //                       CIGAR is empty; score-only prints cigar->score and "-")
 //   --output-full PATH  "plen<TAB>tlen<TAB>score<TAB>pattern<TAB>text<TAB>CIGAR" (:118-142)
 // The score of a full alignment is the CIGAR rescored with the gap-affine penalties
-// (cigar_score_gap_affine), as align_benchmark prints it. Options follow
-// align_benchmark_params.c; configurations other than gap-affine BiWFA without heuristics
-// are refused with exit status 1, as align_benchmark refuses bad options.
+// (cigar_score_gap_affine), or its number of edits for edit-wfa / indel-wfa
+// (cigar_score_edit), as align_benchmark prints it. Options follow align_benchmark_params.c;
+// configurations other than BiWFA without heuristics for those three distances are refused
+// with exit status 1, as align_benchmark refuses bad options.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -38,7 +39,7 @@ struct Options {
   if (msg) fprintf(stderr, "%s\n", msg);
   fprintf(stderr,
           "USE: align_benchmark -i PATH [-o PATH | --output-full PATH] [options]\n"
-          "      --algorithm|a gap-affine-wfa\n"
+          "      --algorithm|a gap-affine-wfa | edit-wfa | indel-wfa\n"
           "      --affine-penalties|g M,X,O,E          (default 0,4,6,2)\n"
           "      --wfa-score-only\n"
           "      --wfa-span global   --wfa-memory ultralow   --wfa-heuristic none\n"
@@ -76,7 +77,8 @@ Options parse(int argc, char** argv) {
     else if (a == "-h" || a == "--help") usage_exit(nullptr);
     else usage_exit((std::string("unknown option ") + a).c_str());
   }
-  if (o.algorithm != "gap-affine-wfa") usage_exit("only --algorithm gap-affine-wfa runs on the GPU aligner");
+  if (o.algorithm != "gap-affine-wfa" && o.algorithm != "edit-wfa" && o.algorithm != "indel-wfa")
+    usage_exit("only --algorithm gap-affine-wfa, edit-wfa or indel-wfa runs on the GPU aligner");
   if (o.memory != "ultralow") usage_exit("only --wfa-memory ultralow (BiWFA) runs on the GPU aligner");
   if (o.heuristic != "none") usage_exit("only --wfa-heuristic none runs on the GPU aligner");
   if (o.span != "global") usage_exit("BiWFA aligns end-to-end only (--wfa-span global)");
@@ -133,8 +135,10 @@ int main(int argc, char** argv) {
   }
   wfg_context_t* ctx = wfg_context_create(opt.device);
   if (!ctx) { fprintf(stderr, "no usable CUDA device %d\n", opt.device); return 1; }
+  const int metric = opt.algorithm == "edit-wfa" ? WFG_METRIC_EDIT
+                   : opt.algorithm == "indel-wfa" ? WFG_METRIC_INDEL : WFG_METRIC_GAP_AFFINE;
   wfg_config_t cfg{opt.match, opt.mismatch, opt.gap_opening, opt.gap_extension, opt.score_only ? 1 : 0,
-                   opt.max_steps};
+                   opt.max_steps, metric};
   Batch b;
   std::vector<int> scores, statuses, run_len;
   std::vector<int64_t> run_off;

@@ -67,7 +67,11 @@ __device__ __forceinline__ WfRef absent_ref() {
   return r;
 }
 
-struct Pen { int x, o, e, scope; };
+// Internal penalties. metric: kMetricAffine, kMetricEdit or kMetricIndel; go: the gap-opening
+// adjust of the overlap and its stop conditions (o for gap-affine, 0 otherwise,
+// wavefront/wavefront_bialign.c:396-410).
+struct Pen { int x, o, e, scope, metric, go; };
+constexpr int kMetricAffine = 0, kMetricEdit = 1, kMetricIndel = 2;
 
 // Oriented window over packed words (forward arrays for the forward aligner and the
 // leaf, reversed arrays for the reverse aligner). bshift = log2(bits per character).
@@ -295,8 +299,109 @@ __device__ __noinline__ int dir_extend(Dir& d, int s, const Grp<G> g, int* max_a
 // range is fixed by which M[k] are in bounds before extension, so the extended offset is
 // written once. Returns -1 on scratch overflow, 1 when the direction is finished (end
 // reached or unreachable), 0 otherwise; *max_ak receives the extension's max antidiagonal.
+// The edit and indel step: wavefront_compute_edit (wavefront/wavefront_compute_edit.c:329-374)
+// with the edit / indel kernels (:41-79), trim, the exact pruning of edit
+// (wavefront_compute_edit_exact_prune, :199-275), then extension and termination as in
+// dir_step. One component (M); the output is [prev.lo-1, prev.hi+1] from the previous score's
+// M wavefront (reads outside its range are null). The component-1 buffer of the output slot
+// keeps the pre-extension offsets the pruning reads.
+template <int G, int MODE>
+__device__ __noinline__ int dir_step_linear(Dir& d, const Pen p, int s, const Grp<G> g, int* max_ak_out) {
+  const DirCfg c = d.cfg;
+  constexpr bool kLeaf = MODE == 1;
+  const int used = d.lused, nphys = d.next_phys;
+  const SeqView sv = d.sv;
+  const uint32_t tl = (uint32_t)sv.tlen, pl = (uint32_t)sv.plen;
+  const bool edit = p.metric == kMetricEdit;
+  *max_ak_out = 0;
+  if (kLeaf && s > c.lmax) return -1;
+  const WfRef pv = ref_raw<MODE>(c, s - 1, 0);  // the previous M wavefront (possibly null)
+  const int lo = pv.lo - 1, hi = pv.hi + 1;
+  const int width = hi - lo + 1;
+  WfRef om, os;  // output M, pre-extension scratch
+  int offm = 0, need = 0;
+  if (!kLeaf) {
+    if (width > c.W) return -1;
+    om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
+    os.base = om.base + c.W;
+    om.kbase = os.kbase = 0;
+    om.mask = os.mask = (uint32_t)c.W - 1u;
+  } else {
+    need = 2 * width;
+    if (used + need > d.lcap) return -1;
+    offm = used;
+    om.base = c.ldata + offm; os.base = om.base + width;
+    om.kbase = os.kbase = lo;
+    om.mask = os.mask = 0xffffffffu;
+  }
+  const int ak = sv.tlen - sv.plen;
+  // r: trimmed lo/hi, max antidiagonal of the extended offsets, min worst-case score
+  int r[4] = {INT_MAX, INT_MIN, 0, INT_MAX};
+  for (int k = lo + g.tid; k <= hi; k += 32 * G) {
+    int32_t m;
+    if (edit) m = max(pv.get(k + 1), max(pv.get(k - 1), pv.get(k)) + 1);
+    else m = max(pv.get(k + 1), pv.get(k - 1) + 1);
+    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
+    os.put(k, m);
+    if (m != kNull) {
+      r[0] = min(r[0], k); r[1] = max(r[1], k);
+      r[3] = min(r[3], max((int)pl - (m - k), (int)tl - m));  // wf_compute_edit_worst_score
+      m += lcp(sv, m - k, m);
+      r[2] = max(r[2], 2 * m - k);
+    }
+    om.put(k, m);
+  }
+  const bool mm[4] = {false, true, true, false};
+  g.minmax(r, mm);
+  g.sync();
+  int nlo = r[0], nhi = r[1];
+  if (nlo > nhi) { nlo = lo; nhi = lo - 1; }  // trimmed to null
+  int max_ak = r[2];
+  if (edit && nhi - nlo + 1 >= 1000) {
+    // Exact pruning. The best case of diagonal k is |k - ak| whatever its offset, the worst
+    // case max(|P| - v, |T| - h); sample the middle diagonal's worst case first.
+    const int sk = nlo + (nhi - nlo) / 2;
+    const int32_t so = os.at(sk);
+    const int smax = (so < 0) ? INT_MAX : max((int)pl - (so - sk), (int)tl - so);
+    if (so >= 0 && (abs(nlo - ak) > smax || abs(nhi - ak) > smax)) {
+      const int mw = r[3];
+      int lo_r, hi_r;
+      const int a = max(nlo, ak - mw), b = min(nhi, ak + mw);
+      lo_r = (a <= b) ? a : nhi + 1;
+      if (lo_r >= nhi) hi_r = nhi;
+      else hi_r = (b > lo_r) ? b : lo_r;
+      if (lo_r != nlo || hi_r != nhi) {
+        // the extension's max antidiagonal covers the pruned range only
+        int q[1] = {0};
+        for (int k = lo_r + g.tid; k <= hi_r; k += 32 * G) {
+          const int32_t m = om.at(k);
+          if (m != kNull) q[0] = max(q[0], 2 * m - k);
+        }
+        const bool mq[1] = {true};
+        g.minmax(q, mq);
+        max_ak = q[0];
+        nlo = lo_r; nhi = hi_r;
+      }
+    }
+  }
+  g.sync();
+  d.num_null = 0;
+  if (kLeaf) d.lused = used + need;
+  else { c.rphys[slot_of(c, s)] = nphys; d.next_phys = (nphys + 1 == c.nphys) ? 0 : nphys + 1; }
+  set_desc<MODE>(c, s, 0, nlo, nhi, offm, lo);
+  set_desc<MODE>(c, s, 1, kAbsent, INT_MIN, 0, 0);
+  set_desc<MODE>(c, s, 2, kAbsent, INT_MIN, 0, 0);
+  // wavefront_termination_end2end on M
+  if (nlo <= ak && ak <= nhi && om.at(ak) >= sv.tlen) {
+    d.status = ST_END_REACHED; d.status_score = s; d.end_k = ak; return 1;
+  }
+  *max_ak_out = max_ak;
+  return 0;
+}
+
 template <int G, int MODE>
 __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g, int* max_ak_out) {
+  if (p.metric != kMetricAffine) return dir_step_linear<G, MODE>(d, p, s, g, max_ak_out);
   const DirCfg c = d.cfg;
   constexpr bool kLeaf = MODE == 1;  // the leaf store (else the modular rings)
   const int nn = d.num_null, used = d.lused, nphys = d.next_phys, ce = d.ce;
@@ -480,7 +585,7 @@ __device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s
   for (int i = 0; i < p.scope; ++i) {
     const int si = s1 - i;
     if (si < 0) break;
-    if (s0 + si - p.o >= bp.score) continue;
+    if (s0 + si - p.go >= bp.score) continue;
     const WfRef dd1 = ref_raw<0>(c1, si, 2);
     if (dd0.present() && dd1.present()) bp_scan<G>(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, g);
     const WfRef ii1 = ref_raw<0>(c1, si, 1);
@@ -550,7 +655,7 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
   for (;;) {
     if (last_fwd) {
       const int min_sr = (sr > p.scope - 1) ? sr - (p.scope - 1) : 0;
-      if (sf + min_sr - p.o >= bp.score) break;
+      if (sf + min_sr - p.go >= bp.score) break;
       overlap<G>(F, R, sf, sr, true, bp, p, g);
       ++sr;
       const int q = dir_step<G, 0>(R, p, sr, g, &ak);
@@ -558,7 +663,7 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
       if (q) return R.status;
     }
     const int min_sf = (sf > p.scope - 1) ? sf - (p.scope - 1) : 0;
-    if (min_sf + sr - p.o >= bp.score) break;
+    if (min_sf + sr - p.go >= bp.score) break;
     overlap<G>(R, F, sr, sf, false, bp, p, g);
     ++sf;
     const int q = dir_step<G, 0>(F, p, sf, g, &ak);
@@ -635,6 +740,7 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
     if (rlen > 0) { if (nrev < lruns_cap) lruns[nrev] = ((uint32_t)rlen << 4) | (uint32_t)rop; else rover = true; ++nrev; }
     rop = op; rlen = len;
   };
+  const bool lin = p.metric != kMetricAffine;
   int matrix = ce, score = s, k = B.end_k;
   int32_t off = tlen;
   int h = off, v = off - k;
@@ -645,14 +751,17 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
   int iters = 0;
   while (v > 0 && h > 0 && score > 0) {
     if (++iters > plen + tlen + 8) return WFG_ST_UNATTAINABLE;
-    const int mm = score - p.x, go = score - p.o - p.e, ge = score - p.e;
+    // gap-affine: wavefront_backtrace_affine; edit/indel: wavefront_backtrace_linear
+    // (wavefront/wavefront_backtrace.c:223-319): M sources only, gap-open = o, no mismatch
+    // source for indel
+    const int mm = score - p.x, go = score - p.o - (lin ? 0 : p.e), ge = score - p.e;
     long long max_all;
     if (matrix == CM) {
-      const long long mis = bt_src(bc, mm, 0, k, 1, BT_M);
+      const long long mis = (p.metric == kMetricIndel) ? (long long)kNull : bt_src(bc, mm, 0, k, 1, BT_M);
       const long long io = bt_src(bc, go, 0, k - 1, 1, BT_I_OPEN);
-      const long long ix = bt_src(bc, ge, 1, k - 1, 1, BT_I_EXT);
+      const long long ix = lin ? (long long)kNull : bt_src(bc, ge, 1, k - 1, 1, BT_I_EXT);
       const long long dop = bt_src(bc, go, 0, k + 1, 0, BT_D_OPEN);
-      const long long dx = bt_src(bc, ge, 2, k + 1, 0, BT_D_EXT);
+      const long long dx = lin ? (long long)kNull : bt_src(bc, ge, 2, k + 1, 0, BT_D_EXT);
       const long long mi = io >= ix ? io : ix;
       const long long md = dop >= dx ? dop : dx;
       const long long mid = mi >= md ? mi : md;
@@ -702,10 +811,13 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
   return ST_OK;
 }
 
-__device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int match, int x, int o, int e) {
+// cigar_score_gap_affine (alignment/cigar.c:277-303), or cigar_score_edit (:244-259) for
+// the edit and indel distances.
+__device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int metric, int match, int x, int o, int e) {
   int score = 0;
   for (int i = 0; i < n; ++i) {
     const int op = (int)(runs[i] & 15u), len = (int)(runs[i] >> 4);
+    if (metric != kMetricAffine) { if (op != WFG_OP_EQ) score += len; continue; }
     if (op == WFG_OP_EQ) score -= match * len;
     else if (op == WFG_OP_X) score -= x * len;
     else score -= o + e * len;
@@ -713,7 +825,8 @@ __device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int mat
   return score;
 }
 
-__device__ __forceinline__ int classic_score(int match_o, int plen, int tlen, int wf_score) {
+__device__ __forceinline__ int classic_score(int metric, int match_o, int plen, int tlen, int wf_score) {
+  if (metric != kMetricAffine) return wf_score;  // indel, edit: the distance itself
   const int swg_match = -match_o;
   if (swg_match == 0) return -wf_score;
   return (swg_match * (plen + tlen) - wf_score) / 2;
@@ -771,7 +884,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
   F.lcap = R.lcap = 0; F.lused = R.lused = 0;
   B.lcap = P.leaf_words; B.lused = 0;
   g.sync();
-  const Pen pen = {P.x, P.o, P.e, P.scope};
+  const Pen pen = {P.x, P.o, P.e, P.scope, P.metric, P.metric == kMetricAffine ? P.o : 0};
 
   const unsigned long long num_pairs =
       P.num_pairs_ptr ? *P.num_pairs_ptr : (unsigned long long)P.num_pairs;
@@ -802,7 +915,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
       const int st = find_breakpoint<G>(F, R, q, 0, q.plen, 0, q.tlen, CM, CM, pen, P.max_steps, bp, g);
       if (st == ST_OK || st == ST_END_REACHED) {
         const int wf = (st == ST_END_REACHED) ? (F.status == ST_END_REACHED ? F.status_score : R.status_score) : bp.score;
-        score = classic_score(P.match_o, q.plen, q.tlen, wf);
+        score = classic_score(P.metric, P.match_o, q.plen, q.tlen, wf);
         status = WFG_ST_COMPLETED;
       } else {
         status = st;
@@ -864,7 +977,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
       if (status == ST_OK) status = WFG_ST_COMPLETED;
       g.sync();
       if (status == WFG_ST_COMPLETED) {
-        score = (out.n > 0) ? rescore_runs(runs, out.n, P.match_o, P.x_o, P.o_o, P.e_o) : 0;
+        score = (out.n > 0) ? rescore_runs(runs, out.n, P.metric, P.match_o, P.x_o, P.o_o, P.e_o) : 0;
         int base_lo = 0, base_hi = 0;
         if (g.tid == 0) {
           const unsigned long long b = atomicAdd(P.out_head, (unsigned long long)out.n);

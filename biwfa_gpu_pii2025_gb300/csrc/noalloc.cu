@@ -142,8 +142,9 @@ extern "C" int wfg_align_noalloc(const wfg_config_t* cfg, int num_pairs, const c
             kMaxPairs);
     return WF_STATUS_UNSUPPORTED;
   }
-  if (cfg->match > 0 || cfg->mismatch <= 0 || cfg->gap_opening < 0 || cfg->gap_extension <= 0) {
-    fprintf(stderr, "[WFA-GB300] wfg_align_noalloc: unsupported penalties\n");
+  if (cfg->metric != WFG_METRIC_GAP_AFFINE || cfg->match > 0 || cfg->mismatch <= 0 || cfg->gap_opening < 0 ||
+      cfg->gap_extension <= 0) {
+    fprintf(stderr, "[WFA-GB300] wfg_align_noalloc: gap-affine penalties with match <= 0 only\n");
     return WF_STATUS_UNSUPPORTED;
   }
   int x, o, e;

@@ -37,7 +37,9 @@ void check_config(AlignerImpl* im) {
   const wavefront_aligner_attr_t& a = im->attr;
   const affine_penalties_t& p = a.affine_penalties;
   im->unsupported = 1;
-  if (a.distance_metric != gap_affine) { im->reason = "only the gap_affine distance is supported"; return; }
+  if (a.distance_metric != gap_affine && a.distance_metric != edit && a.distance_metric != indel) {
+    im->reason = "only the gap_affine, edit and indel distances are supported"; return;
+  }
   if (a.memory_mode != wavefront_memory_ultralow) {
     im->reason = "only wavefront_memory_ultralow (BiWFA) is supported"; return;
   }
@@ -47,7 +49,7 @@ void check_config(AlignerImpl* im) {
       a.alignment_form.text_begin_free || a.alignment_form.text_end_free) {
     im->reason = "BiWFA supports end-to-end alignment only"; return;
   }
-  if (p.match > 0 || p.mismatch <= 0 || p.gap_opening < 0 || p.gap_extension <= 0) {
+  if (a.distance_metric == gap_affine && (p.match > 0 || p.mismatch <= 0 || p.gap_opening < 0 || p.gap_extension <= 0)) {
     im->reason = "penalties must satisfy match <= 0, mismatch > 0, gap_opening >= 0, gap_extension > 0"; return;
   }
   im->unsupported = 0;
@@ -62,6 +64,8 @@ wfg_config_t config_of(const AlignerImpl* im) {
   c.gap_extension = im->attr.affine_penalties.gap_extension;
   c.score_only = im->attr.alignment_scope == compute_score;
   c.max_alignment_steps = im->attr.system.max_alignment_steps;
+  c.metric = (im->attr.distance_metric == edit) ? WFG_METRIC_EDIT
+           : (im->attr.distance_metric == indel) ? WFG_METRIC_INDEL : WFG_METRIC_GAP_AFFINE;
   return c;
 }
 

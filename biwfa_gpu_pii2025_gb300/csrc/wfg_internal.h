@@ -48,6 +48,7 @@ struct KernelParams {
   // penalties: internal (transformed when match < 0) and the caller's for rescoring
   int x, o, e, scope;
   int match_o, x_o, o_o, e_o;
+  int metric;                // 0 gap-affine, 1 edit, 2 indel (x, o, e, scope already set for it)
   int score_only;
   int max_steps;
   // pairs

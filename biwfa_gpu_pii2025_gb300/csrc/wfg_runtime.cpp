@@ -178,6 +178,14 @@ namespace {
 struct IntPen { int x, o, e, scope, nphys; };
 IntPen internal_penalties(const wfg_config_t* cfg) {
   IntPen p;
+  if (cfg->metric == WFG_METRIC_EDIT || cfg->metric == WFG_METRIC_INDEL) {
+    // wavefront_penalties_set_edit / _indel: one component, a wavefront at every score,
+    // max_score_scope 2 (wavefront_components.c:45-60). x bounds the score guard only
+    // (an indel-distance mismatch is two indels).
+    p.x = (cfg->metric == WFG_METRIC_EDIT) ? 1 : 2; p.o = 1; p.e = 1;
+    p.scope = 2; p.nphys = 2;
+    return p;
+  }
   if (cfg->match < 0) {
     p.x = 2 * cfg->mismatch - 2 * cfg->match;
     p.o = 2 * cfg->gap_opening;
@@ -266,7 +274,12 @@ extern "C" {
 
 int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   if (!c || !cfg) return WF_STATUS_UNSUPPORTED;
-  if (cfg->match > 0 || cfg->mismatch <= 0 || cfg->gap_opening < 0 || cfg->gap_extension <= 0) {
+  if (cfg->metric != WFG_METRIC_GAP_AFFINE && cfg->metric != WFG_METRIC_EDIT && cfg->metric != WFG_METRIC_INDEL) {
+    c->err = "unknown distance metric";
+    return WF_STATUS_UNSUPPORTED;
+  }
+  if (cfg->metric == WFG_METRIC_GAP_AFFINE &&
+      (cfg->match > 0 || cfg->mismatch <= 0 || cfg->gap_opening < 0 || cfg->gap_extension <= 0)) {
     c->err = "penalties must satisfy match <= 0, mismatch > 0, gap_opening >= 0, gap_extension > 0";
     return WF_STATUS_UNSUPPORTED;
   }
@@ -400,6 +413,7 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     KernelParams kp{};
     kp.x = p.x; kp.o = p.o; kp.e = p.e; kp.scope = p.scope;
     kp.match_o = cfg->match; kp.x_o = cfg->mismatch; kp.o_o = cfg->gap_opening; kp.e_o = cfg->gap_extension;
+    kp.metric = cfg->metric;
     kp.score_only = cfg->score_only;
     kp.max_steps = cfg->max_alignment_steps > 0 ? cfg->max_alignment_steps : INT_MAX;
     kp.pairs = c->d_pairs.ptr;

@@ -212,10 +212,15 @@ int wavefront_batch_cigar(wavefront_aligner_t* const wf_aligner, const int pair,
  * as WFA2-lib aligners). */
 typedef struct wfg_context wfg_context_t;
 
+/* Distances of wfg_config_t.metric: WFA2-lib's gap_affine (default), edit and indel
+ * (wavefront/wavefront_penalties.c:39-62; the edit and indel distances ignore the penalties). */
+typedef enum { WFG_METRIC_GAP_AFFINE = 0, WFG_METRIC_EDIT = 1, WFG_METRIC_INDEL = 2 } wfg_metric_t;
+
 typedef struct {
   int match, mismatch, gap_opening, gap_extension; /* caller's penalties (match <= 0) */
   int score_only;                                  /* 1: score only (compute_score scope) */
   int max_alignment_steps;                         /* <= 0: unlimited (WFA2 default INT_MAX) */
+  int metric;                                      /* wfg_metric_t; scores of edit/indel are distances */
 } wfg_config_t;
 
 /* Scheduling policy of wfg_run. */

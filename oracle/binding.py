@@ -41,6 +41,9 @@ def build_ref() -> Path | None:
 _orc = None
 _ref = None
 
+# distances (oracle/biwfa_oracle.h ORC_METRIC_*)
+METRIC_AFFINE, METRIC_EDIT, METRIC_INDEL = 0, 1, 2
+
 
 def oracle_lib() -> C.CDLL:
     global _orc
@@ -52,6 +55,9 @@ def oracle_lib() -> C.CDLL:
         lib.orc_biwfa_align.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_int, C.c_int, C.c_char_p, C.c_int, C.POINTER(OrcResult)]
         lib.orc_biwfa_align_batch.restype = C.c_double
+        lib.orc_wfa_align.restype = C.c_int
+        lib.orc_wfa_align.argtypes = [C.c_int] + lib.orc_biwfa_align.argtypes
+        lib.orc_wfa_align_batch.restype = C.c_double
         _orc = lib
     return _orc
 
@@ -63,6 +69,7 @@ def ref_lib() -> C.CDLL | None:
             return None
         lib = C.CDLL(str(REF_SO))
         lib.ref_biwfa_align.restype = C.c_int
+        lib.ref_wfa_align_linear.restype = C.c_int
         _ref = lib
     return _ref
 
@@ -82,19 +89,20 @@ def rle(ops: str) -> str:
     return "".join(out)
 
 
-def oracle_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False):
+def oracle_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False, metric=METRIC_AFFINE):
     """Returns (status, score, ops, OrcResult). score follows align_benchmark's printing:
-    the rescored CIGAR (full mode, -1 when the CIGAR is empty) or cigar->score (score-only)."""
+    the rescored CIGAR (full mode, -1 when the CIGAR is empty) or cigar->score (score-only);
+    for the edit and indel distances the rescoring counts the edits."""
     p, t = _b(pattern), _b(text)
     cap = len(p) + len(t) + 8
     buf = C.create_string_buffer(cap)
     r = OrcResult()
-    st = oracle_lib().orc_biwfa_align(p, len(p), t, len(t), *penalties, 1 if score_only else 0, buf, cap,
-                                      C.byref(r))
+    st = oracle_lib().orc_wfa_align(metric, p, len(p), t, len(t), *penalties, 1 if score_only else 0, buf, cap,
+                                    C.byref(r))
     return st, r.score, buf.raw[:r.ops_len].decode(), r
 
 
-def ref_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False):
+def ref_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False, metric=METRIC_AFFINE):
     """The real WFA2-lib. Returns (status, printed score, ops, cigar->score) or None if unavailable."""
     lib = ref_lib()
     if lib is None:
@@ -104,15 +112,19 @@ def ref_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False):
     cap = len(p) + len(t) + 8
     buf = C.create_string_buffer(cap)
     cs, rs, ol = C.c_int(), C.c_int(), C.c_int()
-    st = lib.ref_biwfa_align(p, len(p), t, len(t), m, x, o, e, 1 if score_only else 0, C.byref(cs), C.byref(rs),
-                             buf, cap, C.byref(ol))
+    if metric == METRIC_AFFINE:
+        st = lib.ref_biwfa_align(p, len(p), t, len(t), m, x, o, e, 1 if score_only else 0, C.byref(cs),
+                                 C.byref(rs), buf, cap, C.byref(ol))
+    else:
+        st = lib.ref_wfa_align_linear(metric, p, len(p), t, len(t), 1 if score_only else 0, C.byref(cs),
+                                      C.byref(rs), buf, cap, C.byref(ol))
     ops = buf.raw[:ol.value].decode()
     score = cs.value if score_only else (rs.value if ops else -1)
     return st, score, ops, cs.value
 
 
 def oracle_batch_time(seq: np.ndarray, p_off, plen, t_off, tlen, penalties=(0, 4, 6, 2), score_only=False,
-                      threads: int = 1, return_ops: bool = False):
+                      threads: int = 1, return_ops: bool = False, metric: int = METRIC_AFFINE):
     """Aligns a batch with the oracle on `threads` POSIX threads; returns (seconds, scores, status[, ops])."""
     lib = oracle_lib()
     n = int(len(plen))
@@ -124,8 +136,8 @@ def oracle_batch_time(seq: np.ndarray, p_off, plen, t_off, tlen, penalties=(0, 4
     ops = np.empty(int((plen.astype(np.int64) + tlen + 1).sum()) + 1, np.uint8)
     scores = np.empty(n, np.int32); status = np.empty(n, np.int32); ops_len = np.empty(n, np.int32)
     i64p, ip = C.POINTER(C.c_int64), C.POINTER(C.c_int)
-    secs = lib.orc_biwfa_align_batch(
-        C.c_int(n), seq.ctypes.data_as(C.c_char_p), p_off.ctypes.data_as(i64p), plen.ctypes.data_as(ip),
+    secs = lib.orc_wfa_align_batch(
+        C.c_int(metric), C.c_int(n), seq.ctypes.data_as(C.c_char_p), p_off.ctypes.data_as(i64p), plen.ctypes.data_as(ip),
         seq.ctypes.data_as(C.c_char_p), t_off.ctypes.data_as(i64p), tlen.ctypes.data_as(ip),
         C.c_int(penalties[0]), C.c_int(penalties[1]), C.c_int(penalties[2]), C.c_int(penalties[3]),
         C.c_int(1 if score_only else 0), ops.ctypes.data_as(C.c_char_p), ops_off.ctypes.data_as(i64p),

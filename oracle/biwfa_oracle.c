@@ -1,7 +1,8 @@
 /*
  * TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT (see biwfa_oracle.h).
  *
- * Plain-C restatement of WFA2-lib v2.3 BiWFA, gap-affine, end-to-end, no heuristic.
+ * Plain-C restatement of WFA2-lib v2.3 BiWFA, end-to-end, no heuristic, for the gap-affine,
+ * edit and indel distances.
  * Every function names the WFA2-lib function (path:line, relative to WFA2-lib/) it
  * restates. Semantics that matter for bit-exact CIGARs and are easy to lose:
  *   - an absent or null input wavefront contributes lo = 1, hi = -1 to the output
@@ -81,8 +82,11 @@ static const int32_t* wf_padded(wf_t* w, int need_lo, int need_hi) {
 }
 
 typedef struct {
-  int x, o, e;        /* internal (possibly transformed) penalties */
-  int scope;          /* max_score_scope = max(o+e, x) + 1 (wavefront_components.c:81-93) */
+  int metric;         /* ORC_METRIC_AFFINE, _EDIT or _INDEL */
+  int x, o, e;        /* internal (possibly transformed) penalties; edit: 1, 1, -; indel: -1, 1, -
+                         (wavefront_penalties_set_edit/_indel, wavefront/wavefront_penalties.c:39-62) */
+  int go_adj;         /* gap-opening adjust of the overlap (wavefront_bialign.c:396-410): o, or 0 */
+  int scope;          /* max_score_scope: max(o+e, x) + 1, or 2 for edit/indel (wavefront_components.c:45-93) */
   int max_steps;      /* system.max_alignment_steps */
 } pen_t;
 
@@ -191,12 +195,85 @@ static void trim_ends(const dir_t* d, wf_t* w) {
   w->lo = k;
 }
 
+/* wf_compute_edit_best_score / _worst_score (wavefront/wavefront_compute_edit.c:199-218) */
+static inline int edit_best(int plen, int tlen, int k, int32_t off) {
+  const int left_v = plen - (off - k), left_h = tlen - off;
+  return left_v >= left_h ? left_v - left_h : left_h - left_v;
+}
+static inline int edit_worst(int plen, int tlen, int k, int32_t off) {
+  const int left_v = plen - (off - k), left_h = tlen - off;
+  return left_v > left_h ? left_v : left_h;
+}
+
+/* wavefront_compute_edit_exact_prune (wavefront/wavefront_compute_edit.c:219-275): on
+ * wavefronts of 1,000 diagonals or more, drop end diagonals whose best case cannot beat the
+ * best worst case. */
+static void edit_prune(const dir_t* d, wf_t* w) {
+  const int plen = d->plen, tlen = d->tlen, lo = w->lo, hi = w->hi;
+  if (hi - lo + 1 < 1000) return;
+  const int32_t* offs = w->off - w->base;
+  const int sample_k = lo + (hi - lo) / 2;
+  if (offs[sample_k] < 0) return;
+  const int smax_sample = edit_worst(plen, tlen, sample_k, offs[sample_k]);
+  if (edit_best(plen, tlen, lo, offs[lo]) <= smax_sample && edit_best(plen, tlen, hi, offs[hi]) <= smax_sample) return;
+  int min_worst = INT_MAX;
+  for (int k = lo; k <= hi; ++k) {
+    if (offs[k] < 0) continue;
+    const int sw = edit_worst(plen, tlen, k, offs[k]);
+    if (sw < min_worst) min_worst = sw;
+  }
+  int lo_r = lo;
+  for (int k = lo; k <= hi; ++k) {
+    if (edit_best(plen, tlen, k, offs[k]) <= min_worst) break;
+    ++lo_r;
+  }
+  int hi_r = hi;
+  for (int k = hi; k > lo_r; --k) {
+    if (edit_best(plen, tlen, k, offs[k]) <= min_worst) break;
+    --hi_r;
+  }
+  w->lo = lo_r; w->hi = hi_r;
+}
+
+/* wavefront_compute_edit (wavefront/wavefront_compute_edit.c:329-374) with the edit and
+ * indel kernels (:41-79): the previous M wavefront, read NULL-padded over [lo-1, hi+1],
+ * gives M over [prev.lo-1, prev.hi+1]; trimmed, then pruned (edit only). */
+static void dir_compute_edit(dir_t* d, int score) {
+  if (!d->modular && score >= d->nslots) dir_grow(d, score + 1 > 2 * d->nslots ? score + 1 : 2 * d->nslots);
+  wf_t* prev = &d->M[dir_slot(d, score - 1)];
+  wf_t* om = &d->M[dir_slot(d, score)];
+  d->cnt->n_steps++;
+  const int lo = prev->lo - 1, hi = prev->hi + 1;
+  const int32_t* pp = wf_padded(prev, lo - 1, hi + 1);
+  wf_reserve(om, lo, hi); om->present = 1; om->lo = lo; om->hi = hi;
+  d->cnt->n_cells += (int64_t)(hi - lo + 1);
+  const uint32_t tl = (uint32_t)d->tlen, pl = (uint32_t)d->plen;
+  int32_t* q = om->off - om->base;
+  const int edit = d->pen->metric == ORC_METRIC_EDIT;
+  for (int k = lo; k <= hi; ++k) {
+    int32_t m;
+    if (edit) {
+      const int32_t ins = pp[k - 1], del = pp[k + 1], mis = pp[k];
+      const int32_t im = (ins >= mis ? ins : mis) + 1;
+      m = del >= im ? del : im;
+    } else {
+      const int32_t ins = pp[k - 1] + 1, del = pp[k + 1];
+      m = del >= ins ? del : ins;
+    }
+    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = OFF_NULL;
+    q[k] = m;
+  }
+  trim_ends(d, om);
+  if (edit) edit_prune(d, om);
+}
+
 /* wavefront_compute_affine (wavefront/wavefront_compute_affine.c:229-260) with
  * fetch_input (wavefront_compute.c:306-352), limits_input (:40-104),
  * allocate_output(_null) (:382-494), the idm kernel (compute_affine.c:44-86)
  * and process_ends (:614-632). */
 static void dir_compute(dir_t* d, int score) {
   const pen_t* p = d->pen;
+  if (p->metric != ORC_METRIC_AFFINE) { dir_compute_edit(d, score); return; }
   if (!d->modular && score >= d->nslots) dir_grow(d, score + 1 > 2 * d->nslots ? score + 1 : 2 * d->nslots);
   wf_t* mx = fetch(d, d->M, score - p->x);
   wf_t* mo = fetch(d, d->M, score - p->o - p->e);
@@ -404,7 +481,7 @@ static void bp_m2m(int plen, int tlen, int fwd, int s0, int s1,
 
 /* wavefront_bialign_overlap (wavefront/wavefront_bialign.c:314-392), gap-affine */
 static void overlap(const ctx_t* c, const dir_t* d0, const dir_t* d1, int s0, int s1, int fwd, bp_t* bp) {
-  const int scope = c->pen.scope, go = c->pen.o;
+  const int scope = c->pen.scope, go = c->pen.go_adj;
   const int plen = d0->plen, tlen = d0->tlen;
   const int sm0 = s0 % scope;
   const wf_t* m0 = &d0->M[sm0];
@@ -460,7 +537,7 @@ static int find_breakpoint(ctx_t* c, int pb, int pe, int tb, int te, int cb, int
     if (qr) return R->status;
     if (sr + sf >= max_steps) return ORC_STATUS_MAX_STEPS_REACHED;
   }
-  const int scope = c->pen.scope, go = c->pen.o;
+  const int scope = c->pen.scope, go = c->pen.go_adj;
   for (;;) {
     if (last_fwd) {
       const int min_sr = (sr > scope - 1) ? sr - (scope - 1) : 0;
@@ -554,6 +631,44 @@ static int backtrace_affine(ctx_t* c, const dir_t* d, int score_end, int k, int3
   return pos + 1;
 }
 
+/* wavefront_backtrace_linear (wavefront/wavefront_backtrace.c:223-319), edit and indel:
+ * sources M[s-x][k] (mismatch, edit only), M[s-o][k-1] (insertion), M[s-o][k+1] (deletion). */
+static int backtrace_linear(ctx_t* c, const dir_t* d, int score_end, int k, int32_t off) {
+  const pen_t* p = &c->pen;
+  char* ops = c->leaf;
+  int pos = c->leaf_cap - 1;
+  int score = score_end;
+  int h = off, v = off - k;
+  if (v < d->plen) { for (int i = d->plen - v; i > 0; --i) ops[pos--] = 'D'; }
+  if (h < d->tlen) { for (int i = d->tlen - h; i > 0; --i) ops[pos--] = 'I'; }
+  while (v > 0 && h > 0 && score > 0) {
+    const int mm = score - p->x, go = score - p->o;
+    const int64_t mis = (p->metric != ORC_METRIC_INDEL) ? bt_src(d, d->M, mm, k, 1, BT_M) : (int64_t)OFF_NULL;
+    const int64_t ins = bt_src(d, d->M, go, k - 1, 1, BT_I_OPEN);
+    const int64_t del = bt_src(d, d->M, go, k + 1, 0, BT_D_OPEN);
+    const int64_t max_all = max64(mis, max64(ins, del));
+    if (max_all < 0) break;
+    const int max_off = (int)(max_all >> 4);
+    for (int i = off - max_off; i > 0; --i) ops[pos--] = 'M';
+    off = max_off;
+    v = off - k; h = off;
+    if (v <= 0 || h <= 0) break;
+    const int type = (int)(max_all & 0xF);
+    if (type == BT_M) { score = mm; ops[pos--] = 'X'; --off; }
+    else if (type == BT_I_OPEN) { score = go; ops[pos--] = 'I'; --k; --off; }
+    else { score = go; ops[pos--] = 'D'; ++k; }
+    v = off - k; h = off;
+  }
+  if (v > 0 && h > 0) {
+    const int nm = v < h ? v : h;
+    for (int i = 0; i < nm; ++i) ops[pos--] = 'M';
+    v -= nm; h -= nm;
+  }
+  while (v > 0) { ops[pos--] = 'D'; --v; }
+  while (h > 0) { ops[pos--] = 'I'; --h; }
+  return pos + 1;
+}
+
 static void append_ops(ctx_t* c, const char* src, int n) {
   if (c->ops != NULL && c->ops_len + n <= c->ops_cap) memcpy(c->ops + c->ops_len, src, (size_t)n);
   c->ops_len += n;
@@ -583,7 +698,8 @@ static int bialign_base(ctx_t* c, int pb, int pe, int tb, int te, int cb, int ce
   const int need = 2 * (B->plen + B->tlen) + 8;
   if (c->leaf_cap < need) { free(c->leaf); c->leaf_cap = need; c->leaf = (char*)malloc((size_t)need); }
   if (B->end_off != OFF_NULL) {
-    const int first = backtrace_affine(c, B, score, B->end_k, B->end_off);
+    const int first = (c->pen.metric == ORC_METRIC_AFFINE) ? backtrace_affine(c, B, score, B->end_k, B->end_off)
+                                                             : backtrace_linear(c, B, score, B->end_k, B->end_off);
     append_ops(c, c->leaf + first, c->leaf_cap - first);
   }
   return ST_OK;
@@ -592,6 +708,7 @@ static int bialign_base(ctx_t* c, int pb, int pe, int tb, int te, int cb, int ce
 static int classic_score(const ctx_t* c, int plen, int tlen, int wf_score) {
   /* wavefront_compute_classic_score (wavefront/wavefront_compute.c:108-120) */
   const int swg_match = -c->match_orig;
+  if (c->pen.metric != ORC_METRIC_AFFINE) return wf_score;  /* indel, edit: the distance itself */
   if (swg_match == 0) return -wf_score;
   return (swg_match * (plen + tlen) - wf_score) / 2; /* WF_SCORE_TO_SW_SCORE */
 }
@@ -623,9 +740,14 @@ static int bialign_alignment(ctx_t* c, int pb, int pe, int tb, int te, int cb, i
   return ST_OK;
 }
 
-/* cigar_score_gap_affine (alignment/cigar.c:277-303) with the caller's penalties. */
-static int rescore(const char* ops, int n, int match, int x, int o, int e) {
+/* cigar_score_gap_affine (alignment/cigar.c:277-303) with the caller's penalties, or
+ * cigar_score_edit (:244-259) for the edit and indel distances. */
+static int rescore(int metric, const char* ops, int n, int match, int x, int o, int e) {
   char last = 0; int score = 0;
+  if (metric != ORC_METRIC_AFFINE) {
+    for (int i = 0; i < n; ++i) score += (ops[i] != 'M');
+    return score;
+  }
   for (int i = 0; i < n; ++i) {
     switch (ops[i]) {
       case 'M': score -= match; break;
@@ -639,17 +761,26 @@ static int rescore(const char* ops, int n, int match, int x, int o, int e) {
   return score;
 }
 
-static void ctx_init(ctx_t* c, int match, int x, int o, int e) {
+static void ctx_init(ctx_t* c, int metric, int match, int x, int o, int e) {
   memset(c, 0, sizeof(*c));
   c->match_orig = match; c->x_orig = x; c->o_orig = o; c->e_orig = e;
-  /* wavefront_penalties_set_affine (wavefront/wavefront_penalties.c:95-130) */
-  if (match < 0) {
-    c->pen.x = 2 * x - 2 * match; c->pen.o = 2 * o; c->pen.e = 2 * e - match;
+  c->pen.metric = metric;
+  if (metric == ORC_METRIC_EDIT || metric == ORC_METRIC_INDEL) {
+    /* wavefront_penalties_set_edit / _indel and wavefront_components_dimensions_edit */
+    c->pen.x = metric == ORC_METRIC_EDIT ? 1 : -1; c->pen.o = 1; c->pen.e = -1;
+    c->pen.go_adj = 0;
+    c->pen.scope = 2;
   } else {
-    c->pen.x = x; c->pen.o = o; c->pen.e = e;
+    /* wavefront_penalties_set_affine (wavefront/wavefront_penalties.c:95-130) */
+    if (match < 0) {
+      c->pen.x = 2 * x - 2 * match; c->pen.o = 2 * o; c->pen.e = 2 * e - match;
+    } else {
+      c->pen.x = x; c->pen.o = o; c->pen.e = e;
+    }
+    const int oe = c->pen.o + c->pen.e;
+    c->pen.scope = (oe > c->pen.x ? oe : c->pen.x) + 1;
+    c->pen.go_adj = c->pen.o;
   }
-  const int oe = c->pen.o + c->pen.e;
-  c->pen.scope = (oe > c->pen.x ? oe : c->pen.x) + 1;
   c->pen.max_steps = INT_MAX;
   c->cnt.max_leaf_score = -1;
   dir_alloc(&c->fwd, &c->pen, &c->cnt, 1, c->pen.scope);
@@ -661,7 +792,9 @@ static void ctx_free(ctx_t* c) {
   free(c->rP); free(c->rT); free(c->leaf);
 }
 
-static int validate(int match, int x, int o, int e) {
+static int validate(int metric, int match, int x, int o, int e) {
+  if (metric == ORC_METRIC_EDIT || metric == ORC_METRIC_INDEL) return 1;
+  if (metric != ORC_METRIC_AFFINE) return 0;
   return !(match > 0 || x <= 0 || o < 0 || e <= 0);
 }
 
@@ -701,25 +834,32 @@ static int align_one(ctx_t* c, const char* pattern, int plen, const char* text, 
     res->ops_len = score_only ? 0 : c->ops_len;
     if (score_only) res->score = c->cigar_score;
     else res->score = (c->ops_len > 0 && c->ops_len <= ops_cap)
-        ? rescore(ops, c->ops_len, c->match_orig, c->x_orig, c->o_orig, c->e_orig) : -1;
+        ? rescore(c->pen.metric, ops, c->ops_len, c->match_orig, c->x_orig, c->o_orig, c->e_orig) : -1;
     res->n_cells = c->cnt.n_cells; res->n_ext = c->cnt.n_ext; res->n_steps = c->cnt.n_steps;
     res->max_leaf_score = c->cnt.max_leaf_score; res->max_depth = c->cnt.max_depth;
   }
   return final_status;
 }
 
-int orc_biwfa_align(const char* pattern, int plen, const char* text, int tlen,
-                    int match, int mismatch, int gap_open, int gap_ext,
-                    int score_only, char* ops, int ops_cap, orc_result_t* res) {
-  if (!validate(match, mismatch, gap_open, gap_ext) || plen < 0 || tlen < 0) {
+int orc_wfa_align(int metric, const char* pattern, int plen, const char* text, int tlen,
+                  int match, int mismatch, int gap_open, int gap_ext,
+                  int score_only, char* ops, int ops_cap, orc_result_t* res) {
+  if (!validate(metric, match, mismatch, gap_open, gap_ext) || plen < 0 || tlen < 0) {
     if (res) { memset(res, 0, sizeof(*res)); res->status = ORC_STATUS_UNATTAINABLE; res->score = -1; }
     return ORC_STATUS_UNATTAINABLE;
   }
   ctx_t c;
-  ctx_init(&c, match, mismatch, gap_open, gap_ext);
+  ctx_init(&c, metric, match, mismatch, gap_open, gap_ext);
   const int st = align_one(&c, pattern, plen, text, tlen, score_only, ops, ops_cap, res);
   ctx_free(&c);
   return st;
+}
+
+int orc_biwfa_align(const char* pattern, int plen, const char* text, int tlen,
+                    int match, int mismatch, int gap_open, int gap_ext,
+                    int score_only, char* ops, int ops_cap, orc_result_t* res) {
+  return orc_wfa_align(ORC_METRIC_AFFINE, pattern, plen, text, tlen, match, mismatch, gap_open, gap_ext, score_only,
+                       ops, ops_cap, res);
 }
 
 /* ---------------------------------------------------------------- batch (CPU baseline) */
@@ -727,7 +867,7 @@ typedef struct {
   int tid, nthreads, n;
   const char* pat; const int64_t* pat_off; const int* plen;
   const char* txt; const int64_t* txt_off; const int* tlen;
-  int match, x, o, e, score_only;
+  int metric, match, x, o, e, score_only;
   char* ops; const int64_t* ops_off;
   int* scores; int* status; int* ops_len;
 } job_t;
@@ -735,7 +875,7 @@ typedef struct {
 static void* batch_worker(void* arg) {
   job_t* j = (job_t*)arg;
   ctx_t c;
-  ctx_init(&c, j->match, j->x, j->o, j->e);
+  ctx_init(&c, j->metric, j->match, j->x, j->o, j->e);
   for (int i = j->tid; i < j->n; i += j->nthreads) {
     orc_result_t r;
     const int cap = j->plen[i] + j->tlen[i] + 1;
@@ -748,19 +888,19 @@ static void* batch_worker(void* arg) {
   return NULL;
 }
 
-double orc_biwfa_align_batch(int n, const char* pat, const int64_t* pat_off, const int* plen,
-                             const char* txt, const int64_t* txt_off, const int* tlen,
-                             int match, int mismatch, int gap_open, int gap_ext, int score_only,
-                             char* ops, const int64_t* ops_off,
-                             int* scores, int* status, int* ops_len, int nthreads) {
+double orc_wfa_align_batch(int metric, int n, const char* pat, const int64_t* pat_off, const int* plen,
+                           const char* txt, const int64_t* txt_off, const int* tlen,
+                           int match, int mismatch, int gap_open, int gap_ext, int score_only,
+                           char* ops, const int64_t* ops_off,
+                           int* scores, int* status, int* ops_len, int nthreads) {
   if (nthreads < 1) nthreads = 1;
-  if (!validate(match, mismatch, gap_open, gap_ext)) return -1.0;
+  if (!validate(metric, match, mismatch, gap_open, gap_ext)) return -1.0;
   pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
   job_t* jobs = (job_t*)malloc(sizeof(job_t) * (size_t)nthreads);
   struct timespec t0, t1;
   clock_gettime(CLOCK_MONOTONIC, &t0);
   for (int t = 0; t < nthreads; ++t) {
-    job_t j = {t, nthreads, n, pat, pat_off, plen, txt, txt_off, tlen, match, mismatch, gap_open, gap_ext,
+    job_t j = {t, nthreads, n, pat, pat_off, plen, txt, txt_off, tlen, metric, match, mismatch, gap_open, gap_ext,
                score_only, ops, ops_off, scores, status, ops_len};
     jobs[t] = j;
     pthread_create(&th[t], NULL, batch_worker, &jobs[t]);
@@ -769,4 +909,13 @@ double orc_biwfa_align_batch(int n, const char* pat, const int64_t* pat_off, con
   clock_gettime(CLOCK_MONOTONIC, &t1);
   free(th); free(jobs);
   return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+double orc_biwfa_align_batch(int n, const char* pat, const int64_t* pat_off, const int* plen,
+                             const char* txt, const int64_t* txt_off, const int* tlen,
+                             int match, int mismatch, int gap_open, int gap_ext, int score_only,
+                             char* ops, const int64_t* ops_off,
+                             int* scores, int* status, int* ops_len, int nthreads) {
+  return orc_wfa_align_batch(ORC_METRIC_AFFINE, n, pat, pat_off, plen, txt, txt_off, tlen, match, mismatch, gap_open,
+                             gap_ext, score_only, ops, ops_off, scores, status, ops_len, nthreads);
 }

@@ -30,6 +30,11 @@ extern "C" {
 #define ORC_STATUS_OOM                (-200)
 #define ORC_STATUS_UNATTAINABLE       (-300)
 
+/* Distances (WFA2-lib's gap_affine, edit, indel); edit and indel ignore the penalties. */
+#define ORC_METRIC_AFFINE 0
+#define ORC_METRIC_EDIT   1
+#define ORC_METRIC_INDEL  2
+
 typedef struct {
   int status;          /* final WFA2 status (0 = completed) */
   int score;           /* full mode: cigar_score_gap_affine() of the ops, -1 if the CIGAR is empty
@@ -49,6 +54,12 @@ int orc_biwfa_align(const char* pattern, int plen, const char* text, int tlen,
                     int match, int mismatch, int gap_open, int gap_ext,
                     int score_only, char* ops, int ops_cap, orc_result_t* res);
 
+/* The same for a given distance (ORC_METRIC_*). For edit and indel, score is the distance
+ * (cigar_score_edit in full mode, as align_benchmark prints it). */
+int orc_wfa_align(int metric, const char* pattern, int plen, const char* text, int tlen,
+                  int match, int mismatch, int gap_open, int gap_ext,
+                  int score_only, char* ops, int ops_cap, orc_result_t* res);
+
 /* Align a batch with nthreads POSIX threads (static interleaved partition).
  * Sequences are concatenated: pattern i is pat[pat_off[i] .. pat_off[i]+plen[i]).
  * ops for pair i go to ops[ops_off[i] ..] (capacity plen+tlen+1 each).
@@ -59,6 +70,11 @@ double orc_biwfa_align_batch(int n, const char* pat, const int64_t* pat_off, con
                              int match, int mismatch, int gap_open, int gap_ext, int score_only,
                              char* ops, const int64_t* ops_off,
                              int* scores, int* status, int* ops_len, int nthreads);
+double orc_wfa_align_batch(int metric, int n, const char* pat, const int64_t* pat_off, const int* plen,
+                           const char* txt, const int64_t* txt_off, const int* tlen,
+                           int match, int mismatch, int gap_open, int gap_ext, int score_only,
+                           char* ops, const int64_t* ops_off,
+                           int* scores, int* status, int* ops_len, int nthreads);
 
 #ifdef __cplusplus
 }

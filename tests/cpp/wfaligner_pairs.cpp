@@ -13,7 +13,8 @@ int main(int argc, char** argv) {
   using wfa::WFAligner;
   if (argc > 1 && std::string(argv[1]) == "--config-only") {
     wfa::WFAlignerGapAffine high(4, 6, 2, WFAligner::Alignment);  // default MemoryHigh
-    wfa::WFAlignerEdit edit(WFAligner::Alignment, WFAligner::MemoryUltralow);
+    wfa::WFAlignerGapAffine2Pieces affine2p(4, 6, 2, 24, 1, WFAligner::Alignment, WFAligner::MemoryUltralow);
+    affine2p.setHeuristicNone();
     wfa::WFAlignerGapAffine dflt(4, 6, 2, WFAligner::Alignment, WFAligner::MemoryUltralow);
     wfa::WFAlignerGapAffine ul(4, 6, 2, WFAligner::Alignment, WFAligner::MemoryUltralow);
     ul.setHeuristicNone();
@@ -21,7 +22,7 @@ int main(int argc, char** argv) {
     std::cout << "no_device\t" << ul.alignEnd2End("", "") << "\n";
     ul.setHeuristicWFadaptive(10, 50);
     std::cout << "high\t" << high.alignEnd2End("ACGT", "ACGA") << "\n";
-    std::cout << "edit\t" << edit.alignEnd2End("ACGT", "ACGA") << "\n";
+    std::cout << "affine2p\t" << affine2p.alignEnd2End("ACGT", "ACGA") << "\n";
     std::cout << "heuristic\t" << ul.alignEnd2End("ACGT", "ACGA") << "\n";
     std::cout << "endsfree\t" << ul.alignEndsFree("ACGT", 0, 0, "ACGA", 0, 0) << "\n";
     std::cout << "status_text\t" << ul.strStatus(WFAligner::StatusUnsupported) << "\n";

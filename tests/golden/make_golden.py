@@ -2,9 +2,10 @@
 
 1. wfa2_utest.json.gz — WFA2-lib's own test vectors for this path, read as text from
    WFA2-lib/tests/: the 305 input pairs (wfa.utest.seq) and the expected `score\\tCIGAR`
-   lines of the BiWFA gap-affine runs (test.biwfa.affine{,.p0..p5}.alg) and the BiWFA
-   score-only runs (test.biwfa.score.affine{,.p0..p5}.alg). Penalties per file follow
-   WFA2-lib/tests/wfa.utest.sh:47-59.
+   lines of the BiWFA gap-affine runs (test.biwfa.affine{,.p0..p5}.alg), the BiWFA
+   score-only runs (test.biwfa.score.affine{,.p0..p5}.alg) and the BiWFA edit and indel
+   runs (test.biwfa{,.score}.{edit,indel}.alg). Penalties per file follow
+   WFA2-lib/tests/wfa.utest.sh:45-59; "metric" is 0 gap-affine, 1 edit, 2 indel.
 2. wfa2_ref_cases.json.gz — outputs of the real WFA2-lib v2.3 (oracle/_ref/libwfa2_ref.so,
    compiled from the reference sources by oracle/Makefile) on seeded synthetic pairs of
    every workload and on edge cases, so the GPU tests can pin parity on the GPU machine where
@@ -43,6 +44,13 @@ UTEST_SETS = {
     "test.biwfa.score.affine.p4.alg": ((-2, 3, 1, 4), True),
     "test.biwfa.score.affine.p5.alg": ((-3, 5, 3, 2), True),
 }
+LINEAR_SETS = {
+    # name: (metric, score_only)
+    "test.biwfa.edit.alg": (1, False),
+    "test.biwfa.indel.alg": (2, False),
+    "test.biwfa.score.edit.alg": (1, True),
+    "test.biwfa.score.indel.alg": (2, True),
+}
 
 
 def read_seq_file(path: Path):
@@ -59,7 +67,10 @@ def make_utest():
     sets = {}
     for name, (pen, score_only) in UTEST_SETS.items():
         lines = (WFA2_TESTS / "wfa.utest.check" / name).read_text().split("\n")[: len(pairs)]
-        sets[name] = {"penalties": list(pen), "score_only": score_only, "lines": lines}
+        sets[name] = {"penalties": list(pen), "score_only": score_only, "metric": 0, "lines": lines}
+    for name, (metric, score_only) in LINEAR_SETS.items():
+        lines = (WFA2_TESTS / "wfa.utest.check" / name).read_text().split("\n")[: len(pairs)]
+        sets[name] = {"penalties": [0, 0, 0, 0], "score_only": score_only, "metric": metric, "lines": lines}
     out = {"source": "WFA2-lib/tests (v2.3)", "pairs": pairs, "sets": sets}
     with gzip.open(HERE / "wfa2_utest.json.gz", "wt") as f:
         json.dump(out, f)
@@ -95,12 +106,13 @@ def make_ref_cases():
         raise SystemExit("oracle/_ref cannot be built: WFA2-lib sources not found")
     cases = []
 
-    def add(tag, pen, score_only, pairs):
+    def add(tag, pen, score_only, pairs, metric=0):
         rows = []
         for p, t in pairs:
-            st, score, ops, cs = binding.ref_align(p, t, pen, score_only)
+            st, score, ops, cs = binding.ref_align(p, t, pen, score_only, metric=metric)
             rows.append([p, t, st, score, binding.rle(ops) if ops else "-"])
-        cases.append({"tag": tag, "penalties": list(pen), "score_only": score_only, "pairs": rows})
+        cases.append({"tag": tag, "penalties": list(pen), "score_only": score_only, "metric": metric,
+                      "pairs": rows})
         print(f"  {tag}: {len(rows)} pairs")
 
     def gen(workload, n, seed):
@@ -116,6 +128,16 @@ def make_ref_cases():
     for pen in [(0, 4, 6, 2), (0, 1, 2, 1), (0, 3, 1, 4), (0, 5, 3, 2), (-5, 1, 2, 1), (-2, 3, 1, 4)]:
         add(f"edge_{'_'.join(map(str, pen))}", pen, False, edges)
     add("edge_score_only", (0, 4, 6, 2), True, edges)
+    # edit and indel distances: generated pairs, edge cases, and pairs of very different
+    # lengths whose wavefronts exceed 1,000 diagonals (edit's exact pruning)
+    rnd = random.Random(77)
+    far = [("".join(rnd.choice("ACGT") for _ in range(a)), "".join(rnd.choice("ACGT") for _ in range(b)))
+           for a, b in ((6000, 1500), (1200, 7000), (4000, 100), (50, 3000))]
+    for metric, name in ((1, "edit"), (2, "indel")):
+        add(f"{name}_w1_1kbp", (0, 0, 0, 0), False, gen(1, 12, 201), metric)
+        add(f"{name}_w3_uneven", (0, 0, 0, 0), False, gen(3, 16, 203), metric)
+        add(f"{name}_edges", (0, 0, 0, 0), False, edges + far, metric)
+        add(f"{name}_score_only", (0, 0, 0, 0), True, gen(5, 32, 205) + far, metric)
     with gzip.open(HERE / "wfa2_ref_cases.json.gz", "wt") as f:
         json.dump({"source": "WFA2-lib v2.3 built from the reference sources (oracle/Makefile ref)",
                    "cases": cases}, f)

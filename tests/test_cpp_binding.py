@@ -42,9 +42,9 @@ def test_cpp_binding_reports_unsupported_configurations(tmp_path):
     out = subprocess.run([str(exe), "--config-only"], capture_output=True, text=True, check=True).stdout
     rows = dict(line.split("\t", 1) for line in out.strip().splitlines())
     unsupported = str(_capi.WF_STATUS_UNSUPPORTED)
-    # MemoryHigh (the binding's default), edit distance, WFA2-lib's default heuristic,
+    # MemoryHigh (the binding's default), two-piece affine, WFA2-lib's default heuristic,
     # an explicit heuristic and ends-free all refuse with a status instead of exiting
-    for key in ("default_heuristic", "high", "edit", "heuristic", "endsfree"):
+    for key in ("default_heuristic", "high", "affine2p", "heuristic", "endsfree"):
         assert rows[key] == unsupported, (key, rows[key])
     assert rows["no_device"] in ("0", str(_capi.WF_STATUS_DEVICE_ERROR))
     assert "not supported" in rows["status_text"]

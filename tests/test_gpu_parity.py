@@ -24,7 +24,8 @@ def test_gpu_matches_wfa2_utest_goldens(batch_aligner, name):
     data = utest()
     s = data["sets"][name]
     b = pkg.PairBatch.from_lists([p for p, _ in data["pairs"]], [t for _, t in data["pairs"]])
-    res = batch_aligner.align(b, penalties=tuple(s["penalties"]), score_only=s["score_only"])
+    res = batch_aligner.align(b, penalties=tuple(s["penalties"]), score_only=s["score_only"],
+                              metric=s.get("metric", 0))
     assert (res.status == 0).all()
     bad = [i for i in range(b.n) if gpu_printed_line(res, i, s["score_only"]) != s["lines"][i]]
     assert not bad, f"{name}: {len(bad)} pairs differ, first {bad[:5]}"
@@ -34,7 +35,8 @@ def test_gpu_matches_wfa2_utest_goldens(batch_aligner, name):
 def test_gpu_matches_wfa2_reference_outputs(batch_aligner, case):
     pairs = case["pairs"]
     b = pkg.PairBatch.from_lists([r[0] for r in pairs], [r[1] for r in pairs])
-    res = batch_aligner.align(b, penalties=tuple(case["penalties"]), score_only=case["score_only"])
+    res = batch_aligner.align(b, penalties=tuple(case["penalties"]), score_only=case["score_only"],
+                              metric=case.get("metric", 0))
     for i, (_, _, st, score, cig) in enumerate(pairs):
         assert res.status[i] == st, i
         assert gpu_printed_line(res, i, case["score_only"]) == printed_line(score, "" if case["score_only"] else
@@ -51,6 +53,60 @@ def test_gpu_matches_oracle_on_generated(batch_aligner, workload, n, seed):
     bad = [i for i in range(b.n) if pkg.runs_to_ops(res.runs_of(i)) != ops[i] or
            res.scores[i] != (scores[i] if ops[i] else 0)]
     assert not bad, f"{len(bad)} pairs differ, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("metric", [_capi.METRIC_EDIT, _capi.METRIC_INDEL], ids=["edit", "indel"])
+@pytest.mark.parametrize("workload,n,seed", [(1, 200, 31), (3, 120, 33), (5, 2000, 35)])
+def test_gpu_linear_distances_match_oracle(batch_aligner, metric, workload, n, seed):
+    """Edit and indel BiWFA (WFA2-lib's edit-wfa / indel-wfa with ultralow memory) against the
+    oracle, full CIGARs and score-only."""
+    b = pkg.PairBatch.generate(workload, n, seed)
+    res = batch_aligner.align(b, metric=metric)
+    res_so = batch_aligner.align(b, metric=metric, score_only=True)
+    _, scores, status, ops = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=8,
+                                                       return_ops=True, metric=metric)
+    _, scores_so, _ = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=8,
+                                                score_only=True, metric=metric)
+    assert (status == 0).all() and (res.status == 0).all() and (res_so.status == 0).all()
+    bad = [i for i in range(b.n) if pkg.runs_to_ops(res.runs_of(i)) != ops[i] or
+           res.scores[i] != (scores[i] if ops[i] else 0) or res_so.scores[i] != scores_so[i]]
+    assert not bad, f"{len(bad)} pairs differ, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("metric", [_capi.METRIC_EDIT, _capi.METRIC_INDEL], ids=["edit", "indel"])
+def test_gpu_linear_distances_through_retry_passes_and_shapes(batch_aligner, metric):
+    """Long pairs of very different lengths (edit's exact pruning), the retry passes of every
+    shape and the multi-warp shapes give the single-warp results."""
+    rng = np.random.default_rng(5)
+    pats, txts = [], []
+    for a, c in ((6000, 1500), (1200, 7000), (3000, 3000), (4000, 100)):
+        pats.append(bytes(rng.choice(list(b"ACGT"), a).astype(np.uint8)))
+        txts.append(bytes(rng.choice(list(b"ACGT"), c).astype(np.uint8)))
+    long_b = pkg.PairBatch.from_lists(pats, txts)
+    mix = pkg.PairBatch.generate(5, 200, seed=36)
+    for b in (long_b, mix):
+        ref = batch_aligner.align(b, metric=metric)
+        for i in range(b.n):
+            st, score, ops, _ = binding.oracle_align(b.pattern(i), b.text(i), metric=metric)
+            assert ref.status[i] == 0 and pkg.runs_to_ops(ref.runs_of(i)) == ops, i
+        outs = []
+        try:
+            batch_aligner.set_arena_limits(ring_w=16, leaf_words=64)
+            for rw in (8, 4, 1):
+                batch_aligner.set_retry_shape(rw)
+                outs.append(batch_aligner.align(b, metric=metric))
+            batch_aligner.set_arena_limits(0, 0)
+            for gw, smem in ((4, False), (8, False), (8, True)):
+                batch_aligner.set_exec_shape(gw, smem)
+                outs.append(batch_aligner.align(b, metric=metric, sched=_capi.SCHED_PLAIN))
+        finally:
+            batch_aligner.set_arena_limits(0, 0)
+            batch_aligner.set_retry_shape(8)
+            batch_aligner.set_exec_shape(1, False)
+        for r in outs:
+            assert np.array_equal(r.status, ref.status) and np.array_equal(r.scores, ref.scores)
+            for i in range(b.n):
+                assert np.array_equal(r.runs_of(i), ref.runs_of(i))
 
 
 def test_gpu_long_noisy_pair_matches_oracle(batch_aligner):

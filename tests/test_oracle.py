@@ -13,10 +13,10 @@ UTEST_NAMES = sorted(utest()["sets"].keys())
 def test_oracle_matches_wfa2_utest_goldens(name):
     data = utest()
     s = data["sets"][name]
-    pen, score_only = tuple(s["penalties"]), s["score_only"]
+    pen, score_only, metric = tuple(s["penalties"]), s["score_only"], s.get("metric", 0)
     bad = []
     for i, (p, t) in enumerate(data["pairs"]):
-        st, score, ops, _ = binding.oracle_align(p, t, pen, score_only)
+        st, score, ops, _ = binding.oracle_align(p, t, pen, score_only, metric=metric)
         line = printed_line(score, "" if score_only else binding.rle(ops))
         if st != 0 or line != s["lines"][i]:
             bad.append(i)
@@ -25,9 +25,9 @@ def test_oracle_matches_wfa2_utest_goldens(name):
 
 @pytest.mark.parametrize("case", ref_cases(), ids=lambda c: c["tag"])
 def test_oracle_matches_wfa2_reference_cases(case):
-    pen, score_only = tuple(case["penalties"]), case["score_only"]
+    pen, score_only, metric = tuple(case["penalties"]), case["score_only"], case.get("metric", 0)
     for p, t, st_ref, score_ref, cig_ref in case["pairs"]:
-        st, score, ops, _ = binding.oracle_align(p, t, pen, score_only)
+        st, score, ops, _ = binding.oracle_align(p, t, pen, score_only, metric=metric)
         assert st == st_ref
         assert score == score_ref
         if not score_only:
@@ -55,9 +55,10 @@ def test_oracle_matches_live_reference_on_random_pairs():
                 del t[pos:pos + int(rng.integers(1, 6))]
         t = "".join(t)
         pen = [(0, 4, 6, 2), (0, 1, 2, 1), (0, 5, 3, 2), (-3, 5, 3, 2)][trial % 4]
-        ref = binding.ref_align(p, t, pen)
-        st, score, ops, _ = binding.oracle_align(p, t, pen)
-        assert (st, score, ops) == (ref[0], ref[1], ref[2]), (p, t, pen)
+        for metric in (binding.METRIC_AFFINE, binding.METRIC_EDIT, binding.METRIC_INDEL):
+            ref = binding.ref_align(p, t, pen, metric=metric)
+            st, score, ops, _ = binding.oracle_align(p, t, pen, metric=metric)
+            assert (st, score, ops) == (ref[0], ref[1], ref[2]), (p, t, pen, metric)
 
 
 def test_oracle_batch_threads_agree_with_single():
