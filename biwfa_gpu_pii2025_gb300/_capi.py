@@ -26,7 +26,7 @@ ALIGNMENT_END2END, ALIGNMENT_ENDSFREE = 0, 1
 WF_HEURISTIC_NONE, WF_HEURISTIC_WFADAPTIVE = 0, 4
 WAVEFRONT_MEMORY_HIGH, WAVEFRONT_MEMORY_ULTRALOW = 0, 3
 SCHED_PLAIN, SCHED_LEARNED, SCHED_GIVEN, SCHED_SORTED = 0, 1, 2, 3
-METRIC_GAP_AFFINE, METRIC_EDIT, METRIC_INDEL = 0, 1, 2
+METRIC_GAP_AFFINE, METRIC_EDIT, METRIC_INDEL, METRIC_GAP_LINEAR = 0, 1, 2, 3
 
 # SAM op codes of the output runs
 OP_INS, OP_DEL, OP_EQ, OP_X = 1, 2, 7, 8

@@ -7,9 +7,10 @@
 //                       CIGAR is empty; score-only prints cigar->score and "-")
 //   --output-full PATH  "plen<TAB>tlen<TAB>score<TAB>pattern<TAB>text<TAB>CIGAR" (:118-142)
 // The score of a full alignment is the CIGAR rescored with the gap-affine penalties
-// (cigar_score_gap_affine), or its number of edits for edit-wfa / indel-wfa
+// (cigar_score_gap_affine), with the linear penalties for gap-linear-wfa
+// (cigar_score_gap_linear), or its number of edits for edit-wfa / indel-wfa
 // (cigar_score_edit), as align_benchmark prints it. Options follow align_benchmark_params.c;
-// configurations other than BiWFA without heuristics for those three distances are refused
+// configurations other than BiWFA without heuristics for those four distances are refused
 // with exit status 1, as align_benchmark refuses bad options.
 #include <chrono>
 #include <cstdio>
@@ -27,6 +28,7 @@ struct Options {
   std::string input, output;
   bool output_full = false;
   int match = 0, mismatch = 4, gap_opening = 6, gap_extension = 2;
+  int lin_match = 0, lin_mismatch = 4, lin_indel = 2;  // --linear-penalties (align_benchmark defaults)
   bool score_only = false;
   std::string span = "global", memory = "ultralow", heuristic = "none";
   int max_steps = 0;
@@ -39,8 +41,9 @@ struct Options {
   if (msg) fprintf(stderr, "%s\n", msg);
   fprintf(stderr,
           "USE: align_benchmark -i PATH [-o PATH | --output-full PATH] [options]\n"
-          "      --algorithm|a gap-affine-wfa | edit-wfa | indel-wfa\n"
+          "      --algorithm|a gap-affine-wfa | gap-linear-wfa | edit-wfa | indel-wfa\n"
           "      --affine-penalties|g M,X,O,E          (default 0,4,6,2)\n"
+          "      --linear-penalties|p M,X,I             (default 0,4,2)\n"
           "      --wfa-score-only\n"
           "      --wfa-span global   --wfa-memory ultralow   --wfa-heuristic none\n"
           "      --wfa-max-steps INT\n"
@@ -66,6 +69,10 @@ Options parse(int argc, char** argv) {
       const char* v = need_value(i, argc, argv);
       if (sscanf(v, "%d,%d,%d,%d", &o.match, &o.mismatch, &o.gap_opening, &o.gap_extension) != 4)
         usage_exit("--affine-penalties expects M,X,O,E");
+    } else if (a == "-p" || a == "--linear-penalties") {
+      const char* v = need_value(i, argc, argv);
+      if (sscanf(v, "%d,%d,%d", &o.lin_match, &o.lin_mismatch, &o.lin_indel) != 3)
+        usage_exit("--linear-penalties expects M,X,I");
     } else if (a == "--wfa-score-only") o.score_only = true;
     else if (a == "--wfa-span") o.span = need_value(i, argc, argv);
     else if (a == "--wfa-memory") o.memory = need_value(i, argc, argv);
@@ -77,8 +84,9 @@ Options parse(int argc, char** argv) {
     else if (a == "-h" || a == "--help") usage_exit(nullptr);
     else usage_exit((std::string("unknown option ") + a).c_str());
   }
-  if (o.algorithm != "gap-affine-wfa" && o.algorithm != "edit-wfa" && o.algorithm != "indel-wfa")
-    usage_exit("only --algorithm gap-affine-wfa, edit-wfa or indel-wfa runs on the GPU aligner");
+  if (o.algorithm != "gap-affine-wfa" && o.algorithm != "gap-linear-wfa" && o.algorithm != "edit-wfa" &&
+      o.algorithm != "indel-wfa")
+    usage_exit("only --algorithm gap-affine-wfa, gap-linear-wfa, edit-wfa or indel-wfa runs on the GPU aligner");
   if (o.memory != "ultralow") usage_exit("only --wfa-memory ultralow (BiWFA) runs on the GPU aligner");
   if (o.heuristic != "none") usage_exit("only --wfa-heuristic none runs on the GPU aligner");
   if (o.span != "global") usage_exit("BiWFA aligns end-to-end only (--wfa-span global)");
@@ -136,9 +144,13 @@ int main(int argc, char** argv) {
   wfg_context_t* ctx = wfg_context_create(opt.device);
   if (!ctx) { fprintf(stderr, "no usable CUDA device %d\n", opt.device); return 1; }
   const int metric = opt.algorithm == "edit-wfa" ? WFG_METRIC_EDIT
-                   : opt.algorithm == "indel-wfa" ? WFG_METRIC_INDEL : WFG_METRIC_GAP_AFFINE;
+                   : opt.algorithm == "indel-wfa" ? WFG_METRIC_INDEL
+                   : opt.algorithm == "gap-linear-wfa" ? WFG_METRIC_GAP_LINEAR : WFG_METRIC_GAP_AFFINE;
   wfg_config_t cfg{opt.match, opt.mismatch, opt.gap_opening, opt.gap_extension, opt.score_only ? 1 : 0,
                    opt.max_steps, metric};
+  if (metric == WFG_METRIC_GAP_LINEAR) {
+    cfg.match = opt.lin_match; cfg.mismatch = opt.lin_mismatch; cfg.gap_opening = opt.lin_indel; cfg.gap_extension = 0;
+  }
   Batch b;
   std::vector<int> scores, statuses, run_len;
   std::vector<int64_t> run_off;

@@ -67,11 +67,11 @@ __device__ __forceinline__ WfRef absent_ref() {
   return r;
 }
 
-// Internal penalties. metric: kMetricAffine, kMetricEdit or kMetricIndel; go: the gap-opening
-// adjust of the overlap and its stop conditions (o for gap-affine, 0 otherwise,
-// wavefront/wavefront_bialign.c:396-410).
+// Internal penalties. metric: kMetricAffine, kMetricEdit, kMetricIndel or kMetricLinear (o =
+// indel, e = 0); go: the gap-opening adjust of the overlap and its stop conditions (o for
+// gap-affine, 0 otherwise, wavefront/wavefront_bialign.c:396-410).
 struct Pen { int x, o, e, scope, metric, go; };
-constexpr int kMetricAffine = 0, kMetricEdit = 1, kMetricIndel = 2;
+constexpr int kMetricAffine = 0, kMetricEdit = 1, kMetricIndel = 2, kMetricLinear = 3;
 
 // Oriented window over packed words (forward arrays for the forward aligner and the
 // leaf, reversed arrays for the reverse aligner). bshift = log2(bits per character).
@@ -401,9 +401,12 @@ __device__ __noinline__ int dir_step_linear(Dir& d, const Pen p, int s, const Gr
 
 template <int G, int MODE>
 __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g, int* max_ak_out) {
-  if (p.metric != kMetricAffine) return dir_step_linear<G, MODE>(d, p, s, g, max_ak_out);
+  if (p.metric == kMetricEdit || p.metric == kMetricIndel) return dir_step_linear<G, MODE>(d, p, s, g, max_ak_out);
   const DirCfg c = d.cfg;
   constexpr bool kLeaf = MODE == 1;  // the leaf store (else the modular rings)
+  // gap-linear (wavefront_compute_linear, wavefront/wavefront_compute_linear.c:166-195): the
+  // same step with M inputs only (mismatch at s-x, indel at s-o) and an M output
+  const bool lin = p.metric == kMetricLinear;
   const int nn = d.num_null, used = d.lused, nphys = d.next_phys, ce = d.ce;
   const SeqView sv = d.sv;
   const uint32_t tl = (uint32_t)sv.tlen, pl = (uint32_t)sv.plen;
@@ -411,8 +414,8 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   if (kLeaf && s > c.lmax) return -1;
   const WfRef mx = fetch<MODE>(c, s - p.x, 0);
   const WfRef mo = fetch<MODE>(c, s - p.o - p.e, 0);
-  const WfRef ie = fetch<MODE>(c, s - p.e, 1);
-  const WfRef de = fetch<MODE>(c, s - p.e, 2);
+  const WfRef ie = lin ? absent_ref() : fetch<MODE>(c, s - p.e, 1);
+  const WfRef de = lin ? absent_ref() : fetch<MODE>(c, s - p.e, 2);
   const bool hx = mx.nonnull(), ho = mo.nonnull(), hie = ie.nonnull(), hde = de.nonnull();
   if (!hx && !ho && !hie && !hde) {
     // null step: no wavefront; the extension finds no M (wavefront_extend_end2end)
@@ -426,9 +429,11 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   }
   int lo = hx ? mx.lo : 1, hi = hx ? mx.hi : -1;
   lo = min(lo, (ho ? mo.lo : 1) - 1);   hi = max(hi, (ho ? mo.hi : -1) + 1);
-  lo = min(lo, (hie ? ie.lo : 1) + 1);  hi = max(hi, (hie ? ie.hi : -1) + 1);
-  lo = min(lo, (hde ? de.lo : 1) - 1);  hi = max(hi, (hde ? de.hi : -1) - 1);
-  const bool ai = ho || hie, ad = ho || hde;
+  if (!lin) {  // wavefront_compute_limits_input stops after M for gap-linear
+    lo = min(lo, (hie ? ie.lo : 1) + 1);  hi = max(hi, (hie ? ie.hi : -1) + 1);
+    lo = min(lo, (hde ? de.lo : 1) - 1);  hi = max(hi, (hde ? de.hi : -1) - 1);
+  }
+  const bool ai = !lin && (ho || hie), ad = !lin && (ho || hde);
   const int width = hi - lo + 1;
   WfRef om, oi, od;
   int offm = 0, offi = 0, offd = 0, need = 0;
@@ -614,7 +619,8 @@ __device__ __forceinline__ SeqView rev_view(const PairSeqs& q, int pb, int pe, i
 // Upper bound on the optimal score of a window (a guard against runaway loops).
 __device__ __forceinline__ int score_guard(const Pen& p, int plen, int tlen) {
   const int mn = min(plen, tlen), df = abs(plen - tlen);
-  const long long b = (long long)p.x * mn + (long long)(p.o + p.e) + (long long)p.e * df + 4LL * p.scope + 16;
+  const int ge = (p.metric == kMetricLinear) ? p.o : p.e;  // cost of one more gap base
+  const long long b = (long long)p.x * mn + (long long)(p.o + p.e) + (long long)ge * df + 4LL * p.scope + 16;
   return (int)min(b, (long long)INT_MAX / 4);
 }
 
@@ -811,13 +817,14 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
   return ST_OK;
 }
 
-// cigar_score_gap_affine (alignment/cigar.c:277-303), or cigar_score_edit (:244-259) for
-// the edit and indel distances.
+// cigar_score_gap_affine (alignment/cigar.c:277-303), cigar_score_gap_linear (:260-276; o is
+// the indel penalty), or cigar_score_edit (:244-259) for the edit and indel distances.
 __device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int metric, int match, int x, int o, int e) {
   int score = 0;
   for (int i = 0; i < n; ++i) {
     const int op = (int)(runs[i] & 15u), len = (int)(runs[i] >> 4);
-    if (metric != kMetricAffine) { if (op != WFG_OP_EQ) score += len; continue; }
+    if (metric == kMetricEdit || metric == kMetricIndel) { if (op != WFG_OP_EQ) score += len; continue; }
+    if (metric == kMetricLinear) { score -= (op == WFG_OP_EQ ? match : op == WFG_OP_X ? x : o) * len; continue; }
     if (op == WFG_OP_EQ) score -= match * len;
     else if (op == WFG_OP_X) score -= x * len;
     else score -= o + e * len;
@@ -826,7 +833,7 @@ __device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int met
 }
 
 __device__ __forceinline__ int classic_score(int metric, int match_o, int plen, int tlen, int wf_score) {
-  if (metric != kMetricAffine) return wf_score;  // indel, edit: the distance itself
+  if (metric == kMetricEdit || metric == kMetricIndel) return wf_score;  // the distance itself
   const int swg_match = -match_o;
   if (swg_match == 0) return -wf_score;
   return (swg_match * (plen + tlen) - wf_score) / 2;

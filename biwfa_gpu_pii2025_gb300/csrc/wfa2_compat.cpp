@@ -37,8 +37,13 @@ void check_config(AlignerImpl* im) {
   const wavefront_aligner_attr_t& a = im->attr;
   const affine_penalties_t& p = a.affine_penalties;
   im->unsupported = 1;
-  if (a.distance_metric != gap_affine && a.distance_metric != edit && a.distance_metric != indel) {
-    im->reason = "only the gap_affine, edit and indel distances are supported"; return;
+  if (a.distance_metric != gap_affine && a.distance_metric != edit && a.distance_metric != indel &&
+      a.distance_metric != gap_linear) {
+    im->reason = "the two-piece affine distance is not supported"; return;
+  }
+  if (a.distance_metric == gap_linear && (a.linear_penalties.match > 0 || a.linear_penalties.mismatch <= 0 ||
+                                          a.linear_penalties.indel <= 0)) {
+    im->reason = "gap-linear penalties must satisfy match <= 0, mismatch > 0, indel > 0"; return;
   }
   if (a.memory_mode != wavefront_memory_ultralow) {
     im->reason = "only wavefront_memory_ultralow (BiWFA) is supported"; return;
@@ -65,7 +70,14 @@ wfg_config_t config_of(const AlignerImpl* im) {
   c.score_only = im->attr.alignment_scope == compute_score;
   c.max_alignment_steps = im->attr.system.max_alignment_steps;
   c.metric = (im->attr.distance_metric == edit) ? WFG_METRIC_EDIT
-           : (im->attr.distance_metric == indel) ? WFG_METRIC_INDEL : WFG_METRIC_GAP_AFFINE;
+           : (im->attr.distance_metric == indel) ? WFG_METRIC_INDEL
+           : (im->attr.distance_metric == gap_linear) ? WFG_METRIC_GAP_LINEAR : WFG_METRIC_GAP_AFFINE;
+  if (c.metric == WFG_METRIC_GAP_LINEAR) {
+    c.match = im->attr.linear_penalties.match;
+    c.mismatch = im->attr.linear_penalties.mismatch;
+    c.gap_opening = im->attr.linear_penalties.indel;
+    c.gap_extension = 0;
+  }
   return c;
 }
 

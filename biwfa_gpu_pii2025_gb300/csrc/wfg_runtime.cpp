@@ -186,6 +186,16 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
     p.scope = 2; p.nphys = 2;
     return p;
   }
+  if (cfg->metric == WFG_METRIC_GAP_LINEAR) {
+    // wavefront_penalties_set_linear (wavefront_penalties.c:63-94), indel from gap_opening;
+    // wavefront_components_dimensions_linear: scope max(x, indel) + 1
+    if (cfg->match < 0) { p.x = 2 * cfg->mismatch - 2 * cfg->match; p.o = 2 * cfg->gap_opening - cfg->match; }
+    else { p.x = cfg->mismatch; p.o = cfg->gap_opening; }
+    p.e = 0;
+    p.scope = std::max(p.x, p.o) + 1;
+    p.nphys = wfg_ring_buffers(p.x, p.o, 0);
+    return p;
+  }
   if (cfg->match < 0) {
     p.x = 2 * cfg->mismatch - 2 * cfg->match;
     p.o = 2 * cfg->gap_opening;
@@ -201,7 +211,7 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
 // Largest score a unidirectional leaf can reach: 500 (END_REACHED recovery) or the
 // optimal score of a whole pair of <= 100 bp (the short-pair fallback).
 int leaf_score_bound(const IntPen& p) {
-  const int short_pair = p.x * 100 + p.o + p.e * 100 + p.scope;
+  const int short_pair = p.x * 100 + p.o + std::max(p.e, p.o) * 100 + p.scope;
   return std::max(520, short_pair) + 8;
 }
 
@@ -274,8 +284,13 @@ extern "C" {
 
 int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   if (!c || !cfg) return WF_STATUS_UNSUPPORTED;
-  if (cfg->metric != WFG_METRIC_GAP_AFFINE && cfg->metric != WFG_METRIC_EDIT && cfg->metric != WFG_METRIC_INDEL) {
+  if (cfg->metric != WFG_METRIC_GAP_AFFINE && cfg->metric != WFG_METRIC_EDIT && cfg->metric != WFG_METRIC_INDEL &&
+      cfg->metric != WFG_METRIC_GAP_LINEAR) {
     c->err = "unknown distance metric";
+    return WF_STATUS_UNSUPPORTED;
+  }
+  if (cfg->metric == WFG_METRIC_GAP_LINEAR && (cfg->match > 0 || cfg->mismatch <= 0 || cfg->gap_opening <= 0)) {
+    c->err = "gap-linear penalties must satisfy match <= 0, mismatch > 0, indel (gap_opening) > 0";
     return WF_STATUS_UNSUPPORTED;
   }
   if (cfg->metric == WFG_METRIC_GAP_AFFINE &&

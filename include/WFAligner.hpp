@@ -12,7 +12,7 @@
  *
  * Header-only; link with -lbiwfa_gb300. Configurations the GPU aligner does not compute
  * (memory models other than MemoryUltralow, heuristics, ends-free and extension forms,
- * distances other than gap-affine, edit and indel, 2-bit packed or lambda sequences) return
+ * the two-piece affine distance, 2-bit packed or lambda sequences) return
  * StatusUnsupported (WF_STATUS_UNSUPPORTED) from the align call instead of computing
  * something different. Like WFA2-lib's, the class is not copyable and not thread-safe:
  * use one aligner per thread. alignEnd2EndBatch() is this library's addition: many pairs
@@ -190,8 +190,7 @@ class WFAligner {
 
   void refresh() {
     unsupported_ = heuristic_unsupported_ ||
-                   (attributes.distance_metric != gap_affine && attributes.distance_metric != edit &&
-                    attributes.distance_metric != indel) ||
+                   attributes.distance_metric == gap_affine_2p ||
                    attributes.memory_mode != wavefront_memory_ultralow;
   }
   AlignmentStatus unsupported() {
@@ -216,8 +215,8 @@ class WFAligner {
   WFAligner& operator=(const WFAligner&) = delete;
 };
 
-// The other distances keep WFA2-lib's class names; edit and indel run on the GPU, gap-linear
-// and two-piece affine aligners report StatusUnsupported.
+// The other distances keep WFA2-lib's class names; indel, edit and gap-linear run on the GPU,
+// two-piece affine aligners report StatusUnsupported.
 class WFAlignerIndel : public WFAligner {
  public:
   WFAlignerIndel(const AlignmentScope alignmentScope, const MemoryModel memoryModel = MemoryHigh)

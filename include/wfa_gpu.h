@@ -212,9 +212,12 @@ int wavefront_batch_cigar(wavefront_aligner_t* const wf_aligner, const int pair,
  * as WFA2-lib aligners). */
 typedef struct wfg_context wfg_context_t;
 
-/* Distances of wfg_config_t.metric: WFA2-lib's gap_affine (default), edit and indel
- * (wavefront/wavefront_penalties.c:39-62; the edit and indel distances ignore the penalties). */
-typedef enum { WFG_METRIC_GAP_AFFINE = 0, WFG_METRIC_EDIT = 1, WFG_METRIC_INDEL = 2 } wfg_metric_t;
+/* Distances of wfg_config_t.metric: WFA2-lib's gap_affine (default), edit, indel and gap_linear
+ * (wavefront/wavefront_penalties.c:39-94). Edit and indel ignore the penalties; gap-linear
+ * takes its indel penalty from gap_opening (match <= 0, mismatch > 0, indel > 0). */
+typedef enum {
+  WFG_METRIC_GAP_AFFINE = 0, WFG_METRIC_EDIT = 1, WFG_METRIC_INDEL = 2, WFG_METRIC_GAP_LINEAR = 3
+} wfg_metric_t;
 
 typedef struct {
   int match, mismatch, gap_opening, gap_extension; /* caller's penalties (match <= 0) */

@@ -42,7 +42,7 @@ _orc = None
 _ref = None
 
 # distances (oracle/biwfa_oracle.h ORC_METRIC_*)
-METRIC_AFFINE, METRIC_EDIT, METRIC_INDEL = 0, 1, 2
+METRIC_AFFINE, METRIC_EDIT, METRIC_INDEL, METRIC_LINEAR = 0, 1, 2, 3
 
 
 def oracle_lib() -> C.CDLL:
@@ -115,6 +115,9 @@ def ref_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False, metric=ME
     if metric == METRIC_AFFINE:
         st = lib.ref_biwfa_align(p, len(p), t, len(t), m, x, o, e, 1 if score_only else 0, C.byref(cs),
                                  C.byref(rs), buf, cap, C.byref(ol))
+    elif metric == METRIC_LINEAR:  # penalties (match, mismatch, indel, -)
+        st = lib.ref_wfa_align_gap_linear(p, len(p), t, len(t), m, x, o, 1 if score_only else 0, C.byref(cs),
+                                          C.byref(rs), buf, cap, C.byref(ol))
     else:
         st = lib.ref_wfa_align_linear(metric, p, len(p), t, len(t), 1 if score_only else 0, C.byref(cs),
                                       C.byref(rs), buf, cap, C.byref(ol))

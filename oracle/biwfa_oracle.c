@@ -2,7 +2,7 @@
  * TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT (see biwfa_oracle.h).
  *
  * Plain-C restatement of WFA2-lib v2.3 BiWFA, end-to-end, no heuristic, for the gap-affine,
- * edit and indel distances.
+ * gap-linear, edit and indel distances.
  * Every function names the WFA2-lib function (path:line, relative to WFA2-lib/) it
  * restates. Semantics that matter for bit-exact CIGARs and are easy to lose:
  *   - an absent or null input wavefront contributes lo = 1, hi = -1 to the output
@@ -82,9 +82,9 @@ static const int32_t* wf_padded(wf_t* w, int need_lo, int need_hi) {
 }
 
 typedef struct {
-  int metric;         /* ORC_METRIC_AFFINE, _EDIT or _INDEL */
-  int x, o, e;        /* internal (possibly transformed) penalties; edit: 1, 1, -; indel: -1, 1, -
-                         (wavefront_penalties_set_edit/_indel, wavefront/wavefront_penalties.c:39-62) */
+  int metric;         /* ORC_METRIC_AFFINE, _LINEAR, _EDIT or _INDEL */
+  int x, o, e;        /* internal (possibly transformed) penalties; gap-linear: x, indel, 0;
+                         edit: 1, 1, -; indel: -1, 1, - (wavefront/wavefront_penalties.c:39-94) */
   int go_adj;         /* gap-opening adjust of the overlap (wavefront_bialign.c:396-410): o, or 0 */
   int scope;          /* max_score_scope: max(o+e, x) + 1, or 2 for edit/indel (wavefront_components.c:45-93) */
   int max_steps;      /* system.max_alignment_steps */
@@ -273,12 +273,15 @@ static void dir_compute_edit(dir_t* d, int score) {
  * and process_ends (:614-632). */
 static void dir_compute(dir_t* d, int score) {
   const pen_t* p = d->pen;
-  if (p->metric != ORC_METRIC_AFFINE) { dir_compute_edit(d, score); return; }
+  if (p->metric == ORC_METRIC_EDIT || p->metric == ORC_METRIC_INDEL) { dir_compute_edit(d, score); return; }
+  /* gap-linear (wavefront_compute_linear, wavefront/wavefront_compute_linear.c:166-195): the
+   * same step with M inputs only (mismatch at s-x, indel at s-o) and an M output */
+  const int lin = p->metric == ORC_METRIC_LINEAR;
   if (!d->modular && score >= d->nslots) dir_grow(d, score + 1 > 2 * d->nslots ? score + 1 : 2 * d->nslots);
   wf_t* mx = fetch(d, d->M, score - p->x);
   wf_t* mo = fetch(d, d->M, score - p->o - p->e);
-  wf_t* ie = fetch(d, d->I, score - p->e);
-  wf_t* de = fetch(d, d->D, score - p->e);
+  wf_t* ie = lin ? NULL : fetch(d, d->I, score - p->e);
+  wf_t* de = lin ? NULL : fetch(d, d->D, score - p->e);
   const int slot = dir_slot(d, score);
   wf_t* om = &d->M[slot]; wf_t* oi = &d->I[slot]; wf_t* od = &d->D[slot];
   d->cnt->n_steps++;
@@ -292,12 +295,14 @@ static void dir_compute(dir_t* d, int score) {
   int lo = mx ? mx->lo : 1, hi = mx ? mx->hi : -1, t;
   t = (mo ? mo->lo : 1) - 1; if (lo > t) lo = t;
   t = (mo ? mo->hi : -1) + 1; if (hi < t) hi = t;
-  t = (ie ? ie->lo : 1) + 1; if (lo > t) lo = t;
-  t = (ie ? ie->hi : -1) + 1; if (hi < t) hi = t;
-  t = (de ? de->lo : 1) - 1; if (lo > t) lo = t;
-  t = (de ? de->hi : -1) - 1; if (hi < t) hi = t;
-  const int alloc_i = (mo != NULL) || (ie != NULL);
-  const int alloc_d = (mo != NULL) || (de != NULL);
+  if (!lin) {  /* wavefront_compute_limits_input stops after M for gap-linear */
+    t = (ie ? ie->lo : 1) + 1; if (lo > t) lo = t;
+    t = (ie ? ie->hi : -1) + 1; if (hi < t) hi = t;
+    t = (de ? de->lo : 1) - 1; if (lo > t) lo = t;
+    t = (de ? de->hi : -1) - 1; if (hi < t) hi = t;
+  }
+  const int alloc_i = !lin && ((mo != NULL) || (ie != NULL));
+  const int alloc_d = !lin && ((mo != NULL) || (de != NULL));
   wf_reserve(om, lo, hi); om->present = 1; om->lo = lo; om->hi = hi;
   if (alloc_i) { wf_reserve(oi, lo, hi); oi->present = 1; oi->lo = lo; oi->hi = hi; } else oi->present = 0;
   if (alloc_d) { wf_reserve(od, lo, hi); od->present = 1; od->lo = lo; od->hi = hi; } else od->present = 0;
@@ -708,7 +713,7 @@ static int bialign_base(ctx_t* c, int pb, int pe, int tb, int te, int cb, int ce
 static int classic_score(const ctx_t* c, int plen, int tlen, int wf_score) {
   /* wavefront_compute_classic_score (wavefront/wavefront_compute.c:108-120) */
   const int swg_match = -c->match_orig;
-  if (c->pen.metric != ORC_METRIC_AFFINE) return wf_score;  /* indel, edit: the distance itself */
+  if (c->pen.metric == ORC_METRIC_EDIT || c->pen.metric == ORC_METRIC_INDEL) return wf_score;  /* the distance */
   if (swg_match == 0) return -wf_score;
   return (swg_match * (plen + tlen) - wf_score) / 2; /* WF_SCORE_TO_SW_SCORE */
 }
@@ -740,12 +745,17 @@ static int bialign_alignment(ctx_t* c, int pb, int pe, int tb, int te, int cb, i
   return ST_OK;
 }
 
-/* cigar_score_gap_affine (alignment/cigar.c:277-303) with the caller's penalties, or
- * cigar_score_edit (:244-259) for the edit and indel distances. */
+/* cigar_score_gap_affine (alignment/cigar.c:277-303) with the caller's penalties,
+ * cigar_score_gap_linear (:260-276, o = indel) or cigar_score_edit (:244-259) for the edit and
+ * indel distances. */
 static int rescore(int metric, const char* ops, int n, int match, int x, int o, int e) {
   char last = 0; int score = 0;
-  if (metric != ORC_METRIC_AFFINE) {
+  if (metric == ORC_METRIC_EDIT || metric == ORC_METRIC_INDEL) {
     for (int i = 0; i < n; ++i) score += (ops[i] != 'M');
+    return score;
+  }
+  if (metric == ORC_METRIC_LINEAR) {
+    for (int i = 0; i < n; ++i) score -= (ops[i] == 'M') ? match : (ops[i] == 'X') ? x : o;
     return score;
   }
   for (int i = 0; i < n; ++i) {
@@ -770,6 +780,14 @@ static void ctx_init(ctx_t* c, int metric, int match, int x, int o, int e) {
     c->pen.x = metric == ORC_METRIC_EDIT ? 1 : -1; c->pen.o = 1; c->pen.e = -1;
     c->pen.go_adj = 0;
     c->pen.scope = 2;
+  } else if (metric == ORC_METRIC_LINEAR) {
+    /* wavefront_penalties_set_linear (wavefront/wavefront_penalties.c:63-94), indel in o;
+     * wavefront_components_dimensions_linear (wavefront_components.c:61-78) */
+    if (match < 0) { c->pen.x = 2 * x - 2 * match; c->pen.o = 2 * o - match; }
+    else { c->pen.x = x; c->pen.o = o; }
+    c->pen.e = 0;
+    c->pen.scope = (c->pen.x > c->pen.o ? c->pen.x : c->pen.o) + 1;
+    c->pen.go_adj = 0;
   } else {
     /* wavefront_penalties_set_affine (wavefront/wavefront_penalties.c:95-130) */
     if (match < 0) {
@@ -794,6 +812,7 @@ static void ctx_free(ctx_t* c) {
 
 static int validate(int metric, int match, int x, int o, int e) {
   if (metric == ORC_METRIC_EDIT || metric == ORC_METRIC_INDEL) return 1;
+  if (metric == ORC_METRIC_LINEAR) return !(match > 0 || x <= 0 || o <= 0);
   if (metric != ORC_METRIC_AFFINE) return 0;
   return !(match > 0 || x <= 0 || o < 0 || e <= 0);
 }

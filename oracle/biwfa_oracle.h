@@ -30,10 +30,12 @@ extern "C" {
 #define ORC_STATUS_OOM                (-200)
 #define ORC_STATUS_UNATTAINABLE       (-300)
 
-/* Distances (WFA2-lib's gap_affine, edit, indel); edit and indel ignore the penalties. */
+/* Distances (WFA2-lib's gap_affine, edit, indel, gap_linear); edit and indel ignore the
+ * penalties, gap-linear reads (match, mismatch, indel) from (match, mismatch, gap_open). */
 #define ORC_METRIC_AFFINE 0
 #define ORC_METRIC_EDIT   1
 #define ORC_METRIC_INDEL  2
+#define ORC_METRIC_LINEAR 3
 
 typedef struct {
   int status;          /* final WFA2 status (0 = completed) */

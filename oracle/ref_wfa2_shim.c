@@ -80,3 +80,36 @@ int ref_wfa_align_linear(int metric, const char* pattern, int plen, const char* 
   wavefront_aligner_delete(wf);
   return status;
 }
+
+/* The same for the gap-linear distance (penalties match, mismatch, indel):
+ * *rescore_out is cigar_score_gap_linear() of the ops, as align_benchmark prints it. */
+int ref_wfa_align_gap_linear(const char* pattern, int plen, const char* text, int tlen, int match, int mismatch,
+                             int indel, int score_only, int* cigar_score_out, int* rescore_out, char* ops_out,
+                             int ops_cap, int* ops_len) {
+  wavefront_aligner_attr_t attr = wavefront_aligner_attr_default;
+  attr.distance_metric = gap_linear;
+  attr.linear_penalties.match = match;
+  attr.linear_penalties.mismatch = mismatch;
+  attr.linear_penalties.indel = indel;
+  attr.memory_mode = wavefront_memory_ultralow;
+  attr.heuristic.strategy = wf_heuristic_none;
+  attr.alignment_scope = score_only ? compute_score : compute_alignment;
+  wavefront_aligner_t* const wf = wavefront_aligner_new(&attr);
+  const int status = wavefront_align(wf, pattern, plen, text, tlen);
+  cigar_t* const cigar = wf->cigar;
+  *cigar_score_out = cigar->score;
+  *ops_len = 0;
+  *rescore_out = -1;
+  if (!score_only && cigar->begin_offset < cigar->end_offset) {
+    const int n = cigar->end_offset - cigar->begin_offset;
+    if (n < ops_cap) {
+      memcpy(ops_out, cigar->operations + cigar->begin_offset, n);
+      ops_out[n] = '\0';
+      *ops_len = n;
+    }
+    linear_penalties_t pen = {match, mismatch, indel};
+    *rescore_out = cigar_score_gap_linear(cigar, &pen);
+  }
+  wavefront_aligner_delete(wf);
+  return status;
+}

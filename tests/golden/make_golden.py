@@ -8,8 +8,9 @@
    WFA2-lib/tests/wfa.utest.sh:45-59; "metric" is 0 gap-affine, 1 edit, 2 indel.
 2. wfa2_ref_cases.json.gz — outputs of the real WFA2-lib v2.3 (oracle/_ref/libwfa2_ref.so,
    compiled from the reference sources by oracle/Makefile) on seeded synthetic pairs of
-   every workload and on edge cases, so the GPU tests can pin parity on the GPU machine where
-   the reference is absent.
+   every workload and on edge cases, for the gap-affine, edit, indel and gap-linear distances
+   ("metric" 0, 1, 2, 3), so the GPU tests can pin parity on the GPU machine where the
+   reference is absent.
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -138,6 +139,12 @@ def make_ref_cases():
         add(f"{name}_w3_uneven", (0, 0, 0, 0), False, gen(3, 16, 203), metric)
         add(f"{name}_edges", (0, 0, 0, 0), False, edges + far, metric)
         add(f"{name}_score_only", (0, 0, 0, 0), True, gen(5, 32, 205) + far, metric)
+    # gap-linear (penalties match, mismatch, indel, -), including match < 0 (Eizenga)
+    for pen in ((0, 4, 2, 0), (0, 1, 1, 0), (-3, 2, 3, 0)):
+        tag = "linear_" + "_".join(map(str, pen[:3]))
+        add(f"{tag}_generated", pen, False, gen(1, 8, 301) + gen(3, 12, 303), 3)
+        add(f"{tag}_edges", pen, False, edges + far[:2], 3)
+        add(f"{tag}_score_only", pen, True, gen(5, 24, 305), 3)
     with gzip.open(HERE / "wfa2_ref_cases.json.gz", "wt") as f:
         json.dump({"source": "WFA2-lib v2.3 built from the reference sources (oracle/Makefile ref)",
                    "cases": cases}, f)

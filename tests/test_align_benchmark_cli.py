@@ -69,3 +69,19 @@ def test_cli_output_full(tmp_path):
     assert rows[0] == ["10", "11", str(score), "ACGTACGTAC", "ACGTTACGTAC", rle] and score == -8
     assert rows[1] == ["0", "3", "-12", "", "ACG", "3I"]
     assert rows[2] == ["7", "7", "0", "GATTACA", "GATTACA", "7M"]
+
+
+@pytest.mark.gpu
+def test_cli_gap_linear_matches_oracle(tmp_path):
+    """gap-linear-wfa with --linear-penalties: every line equals the oracle's (the real WFA2-lib
+    pins the oracle for gap-linear in tests/test_oracle.py)."""
+    exe = _cli()
+    pairs = utest()["pairs"][:150]
+    seq, out = tmp_path / "in.seq", tmp_path / "out.alg"
+    _write_seq(seq, pairs)
+    subprocess.run([exe, "-a", "gap-linear-wfa", "-p", "0,4,2", "-i", str(seq), "-o", str(out), "--wfa-memory",
+                    "ultralow", "--wfa-heuristic", "none", "-q"], check=True)
+    lines = out.read_text().splitlines()
+    for i, (p, t) in enumerate(pairs):
+        st, score, ops, _ = binding.oracle_align(p, t, (0, 4, 2, 0), metric=binding.METRIC_LINEAR)
+        assert lines[i] == (f"{score}\t{binding.rle(ops)}" if ops else "-1\t-"), i

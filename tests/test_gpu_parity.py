@@ -55,17 +55,22 @@ def test_gpu_matches_oracle_on_generated(batch_aligner, workload, n, seed):
     assert not bad, f"{len(bad)} pairs differ, first {bad[:5]}"
 
 
-@pytest.mark.parametrize("metric", [_capi.METRIC_EDIT, _capi.METRIC_INDEL], ids=["edit", "indel"])
+LINEAR_METRICS = [(_capi.METRIC_EDIT, (0, 0, 0, 0)), (_capi.METRIC_INDEL, (0, 0, 0, 0)),
+                  (_capi.METRIC_GAP_LINEAR, (0, 4, 2, 0)), (_capi.METRIC_GAP_LINEAR, (-3, 2, 3, 0))]
+LINEAR_IDS = ["edit", "indel", "gap_linear_0_4_2", "gap_linear_m3_2_3"]
+
+
+@pytest.mark.parametrize("metric,pen", LINEAR_METRICS, ids=LINEAR_IDS)
 @pytest.mark.parametrize("workload,n,seed", [(1, 200, 31), (3, 120, 33), (5, 2000, 35)])
-def test_gpu_linear_distances_match_oracle(batch_aligner, metric, workload, n, seed):
-    """Edit and indel BiWFA (WFA2-lib's edit-wfa / indel-wfa with ultralow memory) against the
-    oracle, full CIGARs and score-only."""
+def test_gpu_linear_distances_match_oracle(batch_aligner, metric, pen, workload, n, seed):
+    """Edit, indel and gap-linear BiWFA (WFA2-lib's edit-wfa / indel-wfa / gap-linear-wfa with
+    ultralow memory) against the oracle, full CIGARs and score-only."""
     b = pkg.PairBatch.generate(workload, n, seed)
-    res = batch_aligner.align(b, metric=metric)
-    res_so = batch_aligner.align(b, metric=metric, score_only=True)
-    _, scores, status, ops = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=8,
+    res = batch_aligner.align(b, penalties=pen, metric=metric)
+    res_so = batch_aligner.align(b, penalties=pen, metric=metric, score_only=True)
+    _, scores, status, ops = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, pen, threads=8,
                                                        return_ops=True, metric=metric)
-    _, scores_so, _ = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=8,
+    _, scores_so, _ = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, pen, threads=8,
                                                 score_only=True, metric=metric)
     assert (status == 0).all() and (res.status == 0).all() and (res_so.status == 0).all()
     bad = [i for i in range(b.n) if pkg.runs_to_ops(res.runs_of(i)) != ops[i] or
@@ -73,8 +78,8 @@ def test_gpu_linear_distances_match_oracle(batch_aligner, metric, workload, n, s
     assert not bad, f"{len(bad)} pairs differ, first {bad[:5]}"
 
 
-@pytest.mark.parametrize("metric", [_capi.METRIC_EDIT, _capi.METRIC_INDEL], ids=["edit", "indel"])
-def test_gpu_linear_distances_through_retry_passes_and_shapes(batch_aligner, metric):
+@pytest.mark.parametrize("metric,pen", LINEAR_METRICS[:3], ids=LINEAR_IDS[:3])
+def test_gpu_linear_distances_through_retry_passes_and_shapes(batch_aligner, metric, pen):
     """Long pairs of very different lengths (edit's exact pruning), the retry passes of every
     shape and the multi-warp shapes give the single-warp results."""
     rng = np.random.default_rng(5)
@@ -85,20 +90,20 @@ def test_gpu_linear_distances_through_retry_passes_and_shapes(batch_aligner, met
     long_b = pkg.PairBatch.from_lists(pats, txts)
     mix = pkg.PairBatch.generate(5, 200, seed=36)
     for b in (long_b, mix):
-        ref = batch_aligner.align(b, metric=metric)
+        ref = batch_aligner.align(b, penalties=pen, metric=metric)
         for i in range(b.n):
-            st, score, ops, _ = binding.oracle_align(b.pattern(i), b.text(i), metric=metric)
+            st, score, ops, _ = binding.oracle_align(b.pattern(i), b.text(i), pen, metric=metric)
             assert ref.status[i] == 0 and pkg.runs_to_ops(ref.runs_of(i)) == ops, i
         outs = []
         try:
             batch_aligner.set_arena_limits(ring_w=16, leaf_words=64)
             for rw in (8, 4, 1):
                 batch_aligner.set_retry_shape(rw)
-                outs.append(batch_aligner.align(b, metric=metric))
+                outs.append(batch_aligner.align(b, penalties=pen, metric=metric))
             batch_aligner.set_arena_limits(0, 0)
             for gw, smem in ((4, False), (8, False), (8, True)):
                 batch_aligner.set_exec_shape(gw, smem)
-                outs.append(batch_aligner.align(b, metric=metric, sched=_capi.SCHED_PLAIN))
+                outs.append(batch_aligner.align(b, penalties=pen, metric=metric, sched=_capi.SCHED_PLAIN))
         finally:
             batch_aligner.set_arena_limits(0, 0)
             batch_aligner.set_retry_shape(8)

@@ -55,10 +55,12 @@ def test_oracle_matches_live_reference_on_random_pairs():
                 del t[pos:pos + int(rng.integers(1, 6))]
         t = "".join(t)
         pen = [(0, 4, 6, 2), (0, 1, 2, 1), (0, 5, 3, 2), (-3, 5, 3, 2)][trial % 4]
-        for metric in (binding.METRIC_AFFINE, binding.METRIC_EDIT, binding.METRIC_INDEL):
-            ref = binding.ref_align(p, t, pen, metric=metric)
-            st, score, ops, _ = binding.oracle_align(p, t, pen, metric=metric)
-            assert (st, score, ops) == (ref[0], ref[1], ref[2]), (p, t, pen, metric)
+        for metric in (binding.METRIC_AFFINE, binding.METRIC_EDIT, binding.METRIC_INDEL, binding.METRIC_LINEAR):
+            # gap-linear reads (match, mismatch, indel) from the first three penalties
+            mpen = (pen[0], pen[1], pen[3] + 1, 0) if metric == binding.METRIC_LINEAR else pen
+            ref = binding.ref_align(p, t, mpen, metric=metric)
+            st, score, ops, _ = binding.oracle_align(p, t, mpen, metric=metric)
+            assert (st, score, ops) == (ref[0], ref[1], ref[2]), (p, t, mpen, metric)
 
 
 def test_oracle_batch_threads_agree_with_single():
