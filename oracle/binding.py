@@ -42,7 +42,13 @@ _orc = None
 _ref = None
 
 # distances (oracle/biwfa_oracle.h ORC_METRIC_*)
-METRIC_AFFINE, METRIC_EDIT, METRIC_INDEL, METRIC_LINEAR = 0, 1, 2, 3
+METRIC_AFFINE, METRIC_EDIT, METRIC_INDEL, METRIC_LINEAR, METRIC_AFFINE2P = 0, 1, 2, 3, 4
+
+
+def pen6(penalties) -> tuple:
+    """(match, mismatch, o1, e1[, o2, e2]) -> the six-entry set; o2/e2 default to (0, 1)."""
+    p = tuple(int(v) for v in penalties)
+    return p + (0, 1)[len(p) - 4:] if len(p) < 6 else p[:6]
 
 
 def oracle_lib() -> C.CDLL:
@@ -58,6 +64,8 @@ def oracle_lib() -> C.CDLL:
         lib.orc_wfa_align.restype = C.c_int
         lib.orc_wfa_align.argtypes = [C.c_int] + lib.orc_biwfa_align.argtypes
         lib.orc_wfa_align_batch.restype = C.c_double
+        lib.orc_wfa_align_pen.restype = C.c_int
+        lib.orc_wfa_align_batch_pen.restype = C.c_double
         _orc = lib
     return _orc
 
@@ -70,6 +78,7 @@ def ref_lib() -> C.CDLL | None:
         lib = C.CDLL(str(REF_SO))
         lib.ref_biwfa_align.restype = C.c_int
         lib.ref_wfa_align_linear.restype = C.c_int
+        lib.ref_wfa_align_affine2p.restype = C.c_int
         _ref = lib
     return _ref
 
@@ -97,8 +106,9 @@ def oracle_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False, metric
     cap = len(p) + len(t) + 8
     buf = C.create_string_buffer(cap)
     r = OrcResult()
-    st = oracle_lib().orc_wfa_align(metric, p, len(p), t, len(t), *penalties, 1 if score_only else 0, buf, cap,
-                                    C.byref(r))
+    pen = (C.c_int * 6)(*pen6(penalties))
+    st = oracle_lib().orc_wfa_align_pen(C.c_int(metric), p, C.c_int(len(p)), t, C.c_int(len(t)), pen,
+                                        C.c_int(1 if score_only else 0), buf, C.c_int(cap), C.byref(r))
     return st, r.score, buf.raw[:r.ops_len].decode(), r
 
 
@@ -107,7 +117,7 @@ def ref_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False, metric=ME
     lib = ref_lib()
     if lib is None:
         return None
-    m, x, o, e = penalties
+    m, x, o, e = penalties[:4]
     p, t = _b(pattern), _b(text)
     cap = len(p) + len(t) + 8
     buf = C.create_string_buffer(cap)
@@ -115,6 +125,10 @@ def ref_align(pattern, text, penalties=(0, 4, 6, 2), score_only=False, metric=ME
     if metric == METRIC_AFFINE:
         st = lib.ref_biwfa_align(p, len(p), t, len(t), m, x, o, e, 1 if score_only else 0, C.byref(cs),
                                  C.byref(rs), buf, cap, C.byref(ol))
+    elif metric == METRIC_AFFINE2P:
+        pen = (C.c_int * 6)(*pen6(penalties))
+        st = lib.ref_wfa_align_affine2p(p, C.c_int(len(p)), t, C.c_int(len(t)), pen, C.c_int(1 if score_only else 0),
+                                        C.byref(cs), C.byref(rs), buf, C.c_int(cap), C.byref(ol))
     elif metric == METRIC_LINEAR:  # penalties (match, mismatch, indel, -)
         st = lib.ref_wfa_align_gap_linear(p, len(p), t, len(t), m, x, o, 1 if score_only else 0, C.byref(cs),
                                           C.byref(rs), buf, cap, C.byref(ol))
@@ -139,10 +153,10 @@ def oracle_batch_time(seq: np.ndarray, p_off, plen, t_off, tlen, penalties=(0, 4
     ops = np.empty(int((plen.astype(np.int64) + tlen + 1).sum()) + 1, np.uint8)
     scores = np.empty(n, np.int32); status = np.empty(n, np.int32); ops_len = np.empty(n, np.int32)
     i64p, ip = C.POINTER(C.c_int64), C.POINTER(C.c_int)
-    secs = lib.orc_wfa_align_batch(
+    pen = (C.c_int * 6)(*pen6(penalties))
+    secs = lib.orc_wfa_align_batch_pen(
         C.c_int(metric), C.c_int(n), seq.ctypes.data_as(C.c_char_p), p_off.ctypes.data_as(i64p), plen.ctypes.data_as(ip),
-        seq.ctypes.data_as(C.c_char_p), t_off.ctypes.data_as(i64p), tlen.ctypes.data_as(ip),
-        C.c_int(penalties[0]), C.c_int(penalties[1]), C.c_int(penalties[2]), C.c_int(penalties[3]),
+        seq.ctypes.data_as(C.c_char_p), t_off.ctypes.data_as(i64p), tlen.ctypes.data_as(ip), pen,
         C.c_int(1 if score_only else 0), ops.ctypes.data_as(C.c_char_p), ops_off.ctypes.data_as(i64p),
         scores.ctypes.data_as(ip), status.ctypes.data_as(ip), ops_len.ctypes.data_as(ip), C.c_int(threads))
     if return_ops:

@@ -2,7 +2,7 @@
  * TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT (see biwfa_oracle.h).
  *
  * Plain-C restatement of WFA2-lib v2.3 BiWFA, end-to-end, no heuristic, for the gap-affine,
- * gap-linear, edit and indel distances.
+ * two-piece gap-affine, gap-linear, edit and indel distances.
  * Every function names the WFA2-lib function (path:line, relative to WFA2-lib/) it
  * restates. Semantics that matter for bit-exact CIGARs and are easy to lose:
  *   - an absent or null input wavefront contributes lo = 1, hi = -1 to the output
@@ -35,10 +35,11 @@
 #define ST_END_UNREACHABLE (-3)
 
 /* Components (alignment/affine2p_penalties.h:51-57) */
-enum { C_M = 0, C_I = 1, C_D = 3 };
+enum { C_M = 0, C_I = 1, C_I2 = 2, C_D = 3, C_D2 = 4 };
 
 /* Backtrace types (wavefront/wavefront_backtrace.c:49-59) */
-enum { BT_M = 9, BT_D_EXT = 6, BT_D_OPEN = 5, BT_I_EXT = 2, BT_I_OPEN = 1 };
+enum { BT_M = 9, BT_D2_EXT = 8, BT_D2_OPEN = 7, BT_D_EXT = 6, BT_D_OPEN = 5, BT_I2_EXT = 4, BT_I2_OPEN = 3,
+       BT_I_EXT = 2, BT_I_OPEN = 1 };
 
 /* ---------------------------------------------------------------- wavefronts */
 typedef struct {
@@ -82,7 +83,8 @@ static const int32_t* wf_padded(wf_t* w, int need_lo, int need_hi) {
 }
 
 typedef struct {
-  int metric;         /* ORC_METRIC_AFFINE, _LINEAR, _EDIT or _INDEL */
+  int metric;         /* ORC_METRIC_AFFINE, _AFFINE2P, _LINEAR, _EDIT or _INDEL */
+  int o2, e2;         /* second gap piece (two-piece affine; wavefront_penalties.c:132-172) */
   int x, o, e;        /* internal (possibly transformed) penalties; gap-linear: x, indel, 0;
                          edit: 1, 1, -; indel: -1, 1, - (wavefront/wavefront_penalties.c:39-94) */
   int go_adj;         /* gap-opening adjust of the overlap (wavefront_bialign.c:396-410): o, or 0 */
@@ -101,7 +103,7 @@ typedef struct {
   counters_t* cnt;
   int modular;              /* ring of `scope` slots (score-only sub-aligners) or one slot per score */
   int nslots;
-  wf_t* M; wf_t* I; wf_t* D;
+  wf_t* M; wf_t* I; wf_t* D; wf_t* I2; wf_t* D2;
   const char* pat; const char* txt; /* oriented window */
   int plen, tlen;
   int comp_begin, comp_end;
@@ -118,22 +120,30 @@ static void dir_alloc(dir_t* d, const pen_t* pen, counters_t* cnt, int modular, 
   d->M = (wf_t*)calloc((size_t)nslots, sizeof(wf_t));
   d->I = (wf_t*)calloc((size_t)nslots, sizeof(wf_t));
   d->D = (wf_t*)calloc((size_t)nslots, sizeof(wf_t));
+  d->I2 = (wf_t*)calloc((size_t)nslots, sizeof(wf_t));
+  d->D2 = (wf_t*)calloc((size_t)nslots, sizeof(wf_t));
 }
 static void dir_grow(dir_t* d, int nslots) {
   if (nslots <= d->nslots) return;
   d->M = (wf_t*)realloc(d->M, sizeof(wf_t) * (size_t)nslots);
   d->I = (wf_t*)realloc(d->I, sizeof(wf_t) * (size_t)nslots);
   d->D = (wf_t*)realloc(d->D, sizeof(wf_t) * (size_t)nslots);
+  d->I2 = (wf_t*)realloc(d->I2, sizeof(wf_t) * (size_t)nslots);
+  d->D2 = (wf_t*)realloc(d->D2, sizeof(wf_t) * (size_t)nslots);
+  memset(d->I2 + d->nslots, 0, sizeof(wf_t) * (size_t)(nslots - d->nslots));
+  memset(d->D2 + d->nslots, 0, sizeof(wf_t) * (size_t)(nslots - d->nslots));
   memset(d->M + d->nslots, 0, sizeof(wf_t) * (size_t)(nslots - d->nslots));
   memset(d->I + d->nslots, 0, sizeof(wf_t) * (size_t)(nslots - d->nslots));
   memset(d->D + d->nslots, 0, sizeof(wf_t) * (size_t)(nslots - d->nslots));
   d->nslots = nslots;
 }
 static void dir_free(dir_t* d) {
-  for (int i = 0; i < d->nslots; ++i) { free(d->M[i].off); free(d->I[i].off); free(d->D[i].off); }
+  for (int i = 0; i < d->nslots; ++i) {
+    free(d->M[i].off); free(d->I[i].off); free(d->D[i].off); free(d->I2[i].off); free(d->D2[i].off);
+  }
   free(d->nullw.off);
   free(d->victim.off);
-  free(d->M); free(d->I); free(d->D);
+  free(d->M); free(d->I); free(d->D); free(d->I2); free(d->D2);
 }
 static inline int dir_slot(const dir_t* d, int score) {
   return d->modular ? score % d->pen->scope : score;
@@ -147,8 +157,10 @@ static void dir_init(dir_t* d, const char* pat, int plen, const char* txt, int t
   d->status = ST_OK; d->status_score = 0;
   d->end_k = INT_MAX; d->end_off = OFF_NULL;
   const int n = d->modular ? d->pen->scope : 1;
-  for (int i = 0; i < n && i < d->nslots; ++i) { d->M[i].present = d->I[i].present = d->D[i].present = 0; }
-  wf_t* w = (cb == C_M) ? &d->M[0] : (cb == C_I) ? &d->I[0] : &d->D[0];
+  for (int i = 0; i < n && i < d->nslots; ++i)
+    d->M[i].present = d->I[i].present = d->D[i].present = d->I2[i].present = d->D2[i].present = 0;
+  wf_t* w = (cb == C_M) ? &d->M[0] : (cb == C_I) ? &d->I[0] : (cb == C_D) ? &d->D[0] : (cb == C_I2) ? &d->I2[0]
+                                                                                                 : &d->D2[0];
   wf_reserve(w, 0, 0);
   w->present = 1; w->lo = 0; w->hi = 0; w->off[0 - w->base] = 0;
 }
@@ -267,6 +279,89 @@ static void dir_compute_edit(dir_t* d, int score) {
   if (edit) edit_prune(d, om);
 }
 
+/* wavefront_compute_affine2p (wavefront/wavefront_compute_affine2p.c:334-368) with the idm
+ * kernel (:44-104): two gap pieces (I1/D1 from M[s-o1-e1] and I1/D1[s-e1], I2/D2 likewise),
+ * limits over all seven inputs, outputs allocated as wavefront_compute_allocate_output does
+ * (wavefront/wavefront_compute.c:450-494), every output trimmed. */
+static void dir_compute_2p(dir_t* d, int score) {
+  const pen_t* p = d->pen;
+  if (!d->modular && score >= d->nslots) dir_grow(d, score + 1 > 2 * d->nslots ? score + 1 : 2 * d->nslots);
+  wf_t* mx = fetch(d, d->M, score - p->x);
+  wf_t* mo1 = fetch(d, d->M, score - p->o - p->e);
+  wf_t* ie1 = fetch(d, d->I, score - p->e);
+  wf_t* de1 = fetch(d, d->D, score - p->e);
+  wf_t* mo2 = fetch(d, d->M, score - p->o2 - p->e2);
+  wf_t* ie2 = fetch(d, d->I2, score - p->e2);
+  wf_t* de2 = fetch(d, d->D2, score - p->e2);
+  const int slot = dir_slot(d, score);
+  wf_t* om = &d->M[slot]; wf_t* oi1 = &d->I[slot]; wf_t* od1 = &d->D[slot];
+  wf_t* oi2 = &d->I2[slot]; wf_t* od2 = &d->D2[slot];
+  d->cnt->n_steps++;
+  if (!mx && !mo1 && !ie1 && !de1 && !mo2 && !ie2 && !de2) {
+    d->num_null_steps++;
+    om->present = oi1->present = od1->present = oi2->present = od2->present = 0;
+    return;
+  }
+  d->num_null_steps = 0;
+  int lo = mx ? mx->lo : 1, hi = mx ? mx->hi : -1, t;
+  t = (mo1 ? mo1->lo : 1) - 1; if (lo > t) lo = t;
+  t = (mo1 ? mo1->hi : -1) + 1; if (hi < t) hi = t;
+  t = (ie1 ? ie1->lo : 1) + 1; if (lo > t) lo = t;
+  t = (ie1 ? ie1->hi : -1) + 1; if (hi < t) hi = t;
+  t = (de1 ? de1->lo : 1) - 1; if (lo > t) lo = t;
+  t = (de1 ? de1->hi : -1) - 1; if (hi < t) hi = t;
+  t = (mo2 ? mo2->lo : 1) - 1; if (lo > t) lo = t;
+  t = (mo2 ? mo2->hi : -1) + 1; if (hi < t) hi = t;
+  t = (ie2 ? ie2->lo : 1) + 1; if (lo > t) lo = t;
+  t = (ie2 ? ie2->hi : -1) + 1; if (hi < t) hi = t;
+  t = (de2 ? de2->lo : 1) - 1; if (lo > t) lo = t;
+  t = (de2 ? de2->hi : -1) - 1; if (hi < t) hi = t;
+  const int a_i1 = mo1 || ie1, a_d1 = mo1 || de1, a_i2 = mo2 || ie2, a_d2 = mo2 || de2;
+  wf_reserve(om, lo, hi); om->present = 1; om->lo = lo; om->hi = hi;
+  wf_t* outs[4] = {oi1, od1, oi2, od2};
+  const int alloc[4] = {a_i1, a_d1, a_i2, a_d2};
+  for (int j = 0; j < 4; ++j) {
+    if (alloc[j]) { wf_reserve(outs[j], lo, hi); outs[j]->present = 1; outs[j]->lo = lo; outs[j]->hi = hi; }
+    else outs[j]->present = 0;
+  }
+  d->cnt->n_cells += 5 * (int64_t)(hi - lo + 1);
+  const uint32_t tl = (uint32_t)d->tlen, pl = (uint32_t)d->plen;
+  /* NULL-padded k-indexed inputs over [lo-1, hi+1] (two inputs may be the same wavefront) */
+  wf_t* ins[7] = {mx, mo1, ie1, de1, mo2, ie2, de2};
+  const int32_t* pin[7];
+  for (int j = 0; j < 7; ++j) {
+    int shared = -1;
+    for (int q = 0; q < j; ++q) if (ins[j] != NULL && ins[q] == ins[j]) shared = q;
+    pin[j] = ins[j] ? (shared >= 0 ? pin[shared] : wf_padded(ins[j], lo - 1, hi + 1)) : null_padded(d, lo - 1, hi + 1);
+  }
+  for (int j = 0; j < 7; ++j) if (!ins[j]) pin[j] = null_padded(d, lo - 1, hi + 1);
+  wf_reserve(&d->victim, lo, hi);
+  int32_t* const vic = d->victim.off - d->victim.base;
+  int32_t* qm = om->off - om->base;
+  int32_t* q[4];
+  for (int j = 0; j < 4; ++j) q[j] = alloc[j] ? outs[j]->off - outs[j]->base : vic;
+  for (int k = lo; k <= hi; ++k) {
+    const int32_t i1o = pin[1][k - 1], i1e = pin[2][k - 1];
+    const int32_t ins1 = (i1o >= i1e ? i1o : i1e) + 1;
+    const int32_t i2o = pin[4][k - 1], i2e = pin[5][k - 1];
+    const int32_t ins2 = (i2o >= i2e ? i2o : i2e) + 1;
+    const int32_t ins = ins1 >= ins2 ? ins1 : ins2;
+    const int32_t d1o = pin[1][k + 1], d1e = pin[3][k + 1];
+    const int32_t del1 = d1o >= d1e ? d1o : d1e;
+    const int32_t d2o = pin[4][k + 1], d2e = pin[6][k + 1];
+    const int32_t del2 = d2o >= d2e ? d2o : d2e;
+    const int32_t del = del1 >= del2 ? del1 : del2;
+    const int32_t mis = pin[0][k] + 1;
+    int32_t m = mis >= ins ? mis : ins;
+    m = del >= m ? del : m;
+    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = OFF_NULL;
+    q[0][k] = ins1; q[1][k] = del1; q[2][k] = ins2; q[3][k] = del2;
+    qm[k] = m;
+  }
+  trim_ends(d, om);
+  for (int j = 0; j < 4; ++j) if (alloc[j]) trim_ends(d, outs[j]);
+}
+
 /* wavefront_compute_affine (wavefront/wavefront_compute_affine.c:229-260) with
  * fetch_input (wavefront_compute.c:306-352), limits_input (:40-104),
  * allocate_output(_null) (:382-494), the idm kernel (compute_affine.c:44-86)
@@ -274,6 +369,7 @@ static void dir_compute_edit(dir_t* d, int score) {
 static void dir_compute(dir_t* d, int score) {
   const pen_t* p = d->pen;
   if (p->metric == ORC_METRIC_EDIT || p->metric == ORC_METRIC_INDEL) { dir_compute_edit(d, score); return; }
+  if (p->metric == ORC_METRIC_AFFINE2P) { dir_compute_2p(d, score); return; }
   /* gap-linear (wavefront_compute_linear, wavefront/wavefront_compute_linear.c:166-195): the
    * same step with M inputs only (mismatch at s-x, indel at s-o) and an M output */
   const int lin = p->metric == ORC_METRIC_LINEAR;
@@ -366,7 +462,8 @@ static int termination(dir_t* d, int score) {
   const int ak = d->tlen - d->plen;
   const int aoff = d->tlen;
   const int slot = dir_slot(d, score);
-  const wf_t* w = (d->comp_end == C_M) ? &d->M[slot] : (d->comp_end == C_I) ? &d->I[slot] : &d->D[slot];
+  const wf_t* w = (d->comp_end == C_M) ? &d->M[slot] : (d->comp_end == C_I) ? &d->I[slot]
+                 : (d->comp_end == C_D) ? &d->D[slot] : (d->comp_end == C_I2) ? &d->I2[slot] : &d->D2[slot];
   if (!w->present || w->lo > ak || ak > w->hi) return 0;
   if (w->off[ak - w->base] < aoff) return 0;
   d->end_k = ak; d->end_off = aoff;
@@ -415,7 +512,7 @@ typedef struct {
 
 typedef struct {
   pen_t pen;
-  int match_orig, x_orig, o_orig, e_orig;
+  int match_orig, x_orig, o_orig, e_orig, o2_orig, e2_orig;
   const char* P; const char* T; /* forward full sequences */
   char* rP; char* rT;           /* reversed full sequences */
   int plen_full, tlen_full;
@@ -428,9 +525,8 @@ typedef struct {
 } ctx_t;
 
 /* wavefront_bialign_breakpoint_indel2indel (wavefront/wavefront_bialign.c:189-256) */
-static void bp_indel(const ctx_t* c, int plen, int tlen, int fwd, int s0, int s1,
+static void bp_indel(int go, int plen, int tlen, int fwd, int s0, int s1,
                      const wf_t* w0, const wf_t* w1, int comp, bp_t* bp) {
-  const int go = c->pen.o;
   const int lo0 = w0->lo, hi0 = w0->hi;
   const int lo1 = tlen - plen - w1->hi, hi1 = tlen - plen - w1->lo;
   if (hi1 < lo0 || hi0 < lo1) return;
@@ -484,24 +580,35 @@ static void bp_m2m(int plen, int tlen, int fwd, int s0, int s1,
   }
 }
 
-/* wavefront_bialign_overlap (wavefront/wavefront_bialign.c:314-392), gap-affine */
+/* wavefront_bialign_overlap (wavefront/wavefront_bialign.c:314-392): the second gap
+ * piece's I2/D2 pairs first (gap-open o2), then I1/D1 (o1), then M. */
 static void overlap(const ctx_t* c, const dir_t* d0, const dir_t* d1, int s0, int s1, int fwd, bp_t* bp) {
   const int scope = c->pen.scope, go = c->pen.go_adj;
   const int plen = d0->plen, tlen = d0->tlen;
   const int sm0 = s0 % scope;
   const wf_t* m0 = &d0->M[sm0];
   if (!m0->present) return;
+  const int two = c->pen.metric == ORC_METRIC_AFFINE2P;
   const wf_t* dd0 = &d0->D[sm0];
   const wf_t* ii0 = &d0->I[sm0];
+  const wf_t* dd20 = two ? &d0->D2[sm0] : NULL;
+  const wf_t* ii20 = two ? &d0->I2[sm0] : NULL;
   for (int i = 0; i < scope; ++i) {
     const int si = s1 - i;
     if (si < 0) break;
     const int smi = si % scope;
-    if (s0 + si - go >= bp->score) continue;
+    if (two) {
+      if (s0 + si - c->pen.o2 >= bp->score) continue;
+      const wf_t* dd21 = &d1->D2[smi];
+      if (dd20->present && dd21->present) bp_indel(c->pen.o2, plen, tlen, fwd, s0, si, dd20, dd21, C_D2, bp);
+      const wf_t* ii21 = &d1->I2[smi];
+      if (ii20->present && ii21->present) bp_indel(c->pen.o2, plen, tlen, fwd, s0, si, ii20, ii21, C_I2, bp);
+    }
+    if (s0 + si - (two ? c->pen.o : go) >= bp->score) continue;
     const wf_t* dd1 = &d1->D[smi];
-    if (dd0->present && dd1->present) bp_indel(c, plen, tlen, fwd, s0, si, dd0, dd1, C_D, bp);
+    if (dd0->present && dd1->present) bp_indel(c->pen.o, plen, tlen, fwd, s0, si, dd0, dd1, C_D, bp);
     const wf_t* ii1 = &d1->I[smi];
-    if (ii0->present && ii1->present) bp_indel(c, plen, tlen, fwd, s0, si, ii0, ii1, C_I, bp);
+    if (ii0->present && ii1->present) bp_indel(c->pen.o, plen, tlen, fwd, s0, si, ii0, ii1, C_I, bp);
     if (s0 + si >= bp->score) continue;
     const wf_t* mm1 = &d1->M[smi];
     if (mm1->present) bp_m2m(plen, tlen, fwd, s0, si, m0, mm1, bp);
@@ -574,7 +681,8 @@ static inline int64_t bt_src(const dir_t* d, const wf_t* comp, int score, int kk
 }
 static inline int64_t max64(int64_t a, int64_t b) { return a >= b ? a : b; }
 
-/* wavefront_backtrace_affine (wavefront/wavefront_backtrace.c:320-529), gap-affine.
+/* wavefront_backtrace_affine (wavefront/wavefront_backtrace.c:320-529), gap-affine and
+ * two-piece gap-affine.
  * Writes the ops of the leaf into c->leaf backwards; returns the first index. */
 static int backtrace_affine(ctx_t* c, const dir_t* d, int score_end, int k, int32_t off) {
   const pen_t* p = &c->pen;
@@ -589,6 +697,7 @@ static int backtrace_affine(ctx_t* c, const dir_t* d, int score_end, int k, int3
   }
   while (v > 0 && h > 0 && score > 0) {
     const int mm = score - p->x, go = score - p->o - p->e, ge = score - p->e;
+    const int go2 = score - p->o2 - p->e2, ge2 = score - p->e2;
     int64_t max_all;
     if (matrix == C_M) {
       const int64_t mis = bt_src(d, d->M, mm, k, 1, BT_M);
@@ -596,11 +705,25 @@ static int backtrace_affine(ctx_t* c, const dir_t* d, int score_end, int k, int3
       const int64_t ix = bt_src(d, d->I, ge, k - 1, 1, BT_I_EXT);
       const int64_t dop = bt_src(d, d->M, go, k + 1, 0, BT_D_OPEN);
       const int64_t dx = bt_src(d, d->D, ge, k + 1, 0, BT_D_EXT);
-      max_all = max64(mis, max64(max64(io, ix), max64(dop, dx)));
+      if (p->metric == ORC_METRIC_AFFINE2P) {
+        const int64_t io2 = bt_src(d, d->M, go2, k - 1, 1, BT_I2_OPEN);
+        const int64_t ix2 = bt_src(d, d->I2, ge2, k - 1, 1, BT_I2_EXT);
+        const int64_t dop2 = bt_src(d, d->M, go2, k + 1, 0, BT_D2_OPEN);
+        const int64_t dx2 = bt_src(d, d->D2, ge2, k + 1, 0, BT_D2_EXT);
+        const int64_t ins = max64(max64(io, ix), max64(io2, ix2));
+        const int64_t del = max64(max64(dop, dx), max64(dop2, dx2));
+        max_all = max64(mis, max64(ins, del));
+      } else {
+        max_all = max64(mis, max64(max64(io, ix), max64(dop, dx)));
+      }
     } else if (matrix == C_I) {
       max_all = max64(bt_src(d, d->M, go, k - 1, 1, BT_I_OPEN), bt_src(d, d->I, ge, k - 1, 1, BT_I_EXT));
-    } else {
+    } else if (matrix == C_I2) {
+      max_all = max64(bt_src(d, d->M, go2, k - 1, 1, BT_I2_OPEN), bt_src(d, d->I2, ge2, k - 1, 1, BT_I2_EXT));
+    } else if (matrix == C_D) {
       max_all = max64(bt_src(d, d->M, go, k + 1, 0, BT_D_OPEN), bt_src(d, d->D, ge, k + 1, 0, BT_D_EXT));
+    } else {
+      max_all = max64(bt_src(d, d->M, go2, k + 1, 0, BT_D2_OPEN), bt_src(d, d->D2, ge2, k + 1, 0, BT_D2_EXT));
     }
     if (max_all < 0) break;
     if (matrix == C_M) {
@@ -617,10 +740,16 @@ static int backtrace_affine(ctx_t* c, const dir_t* d, int score_end, int k, int3
       case BT_I_OPEN: score = go; matrix = C_M; break;
       case BT_I_EXT: score = ge; matrix = C_I; break;
       case BT_D_OPEN: score = go; matrix = C_M; break;
-      default: score = ge; matrix = C_D; break; /* BT_D_EXT */
+      case BT_D_EXT: score = ge; matrix = C_D; break;
+      case BT_I2_OPEN: score = go2; matrix = C_M; break;
+      case BT_I2_EXT: score = ge2; matrix = C_I2; break;
+      case BT_D2_OPEN: score = go2; matrix = C_M; break;
+      default: score = ge2; matrix = C_D2; break; /* BT_D2_EXT */
     }
     if (type == BT_M) { ops[pos--] = 'X'; --off; }
-    else if (type == BT_I_OPEN || type == BT_I_EXT) { ops[pos--] = 'I'; --k; --off; }
+    else if (type == BT_I_OPEN || type == BT_I_EXT || type == BT_I2_OPEN || type == BT_I2_EXT) {
+      ops[pos--] = 'I'; --k; --off;
+    }
     else { ops[pos--] = 'D'; ++k; }
     v = off - k; h = off;
   }
@@ -703,7 +832,7 @@ static int bialign_base(ctx_t* c, int pb, int pe, int tb, int te, int cb, int ce
   const int need = 2 * (B->plen + B->tlen) + 8;
   if (c->leaf_cap < need) { free(c->leaf); c->leaf_cap = need; c->leaf = (char*)malloc((size_t)need); }
   if (B->end_off != OFF_NULL) {
-    const int first = (c->pen.metric == ORC_METRIC_AFFINE) ? backtrace_affine(c, B, score, B->end_k, B->end_off)
+    const int first = (c->pen.metric == ORC_METRIC_AFFINE || c->pen.metric == ORC_METRIC_AFFINE2P) ? backtrace_affine(c, B, score, B->end_k, B->end_off)
                                                              : backtrace_linear(c, B, score, B->end_k, B->end_off);
     append_ops(c, c->leaf + first, c->leaf_cap - first);
   }
@@ -745,11 +874,25 @@ static int bialign_alignment(ctx_t* c, int pb, int pe, int tb, int te, int cb, i
   return ST_OK;
 }
 
-/* cigar_score_gap_affine (alignment/cigar.c:277-303) with the caller's penalties,
+/* cigar_score_gap_affine2p (alignment/cigar.c:304-342: per run of I or D the cheaper piece,
+ * min(o1 + e1*L, o2 + e2*L)),
+ * cigar_score_gap_affine (alignment/cigar.c:277-303) with the caller's penalties,
  * cigar_score_gap_linear (:260-276, o = indel) or cigar_score_edit (:244-259) for the edit and
  * indel distances. */
-static int rescore(int metric, const char* ops, int n, int match, int x, int o, int e) {
+static int rescore(int metric, const char* ops, int n, int match, int x, int o, int e, int o2, int e2) {
   char last = 0; int score = 0;
+  if (metric == ORC_METRIC_AFFINE2P) {
+    for (int i = 0; i < n;) {
+      int j = i;
+      while (j < n && ops[j] == ops[i]) ++j;
+      const int len = j - i;
+      if (ops[i] == 'M') score -= match * len;
+      else if (ops[i] == 'X') score -= x * len;
+      else { const int a = o + e * len, b = o2 + e2 * len; score -= a < b ? a : b; }
+      i = j;
+    }
+    return score;
+  }
   if (metric == ORC_METRIC_EDIT || metric == ORC_METRIC_INDEL) {
     for (int i = 0; i < n; ++i) score += (ops[i] != 'M');
     return score;
@@ -771,9 +914,9 @@ static int rescore(int metric, const char* ops, int n, int match, int x, int o, 
   return score;
 }
 
-static void ctx_init(ctx_t* c, int metric, int match, int x, int o, int e) {
+static void ctx_init(ctx_t* c, int metric, int match, int x, int o, int e, int o2, int e2) {
   memset(c, 0, sizeof(*c));
-  c->match_orig = match; c->x_orig = x; c->o_orig = o; c->e_orig = e;
+  c->match_orig = match; c->x_orig = x; c->o_orig = o; c->e_orig = e; c->o2_orig = o2; c->e2_orig = e2;
   c->pen.metric = metric;
   if (metric == ORC_METRIC_EDIT || metric == ORC_METRIC_INDEL) {
     /* wavefront_penalties_set_edit / _indel and wavefront_components_dimensions_edit */
@@ -788,6 +931,21 @@ static void ctx_init(ctx_t* c, int metric, int match, int x, int o, int e) {
     c->pen.e = 0;
     c->pen.scope = (c->pen.x > c->pen.o ? c->pen.x : c->pen.o) + 1;
     c->pen.go_adj = 0;
+  } else if (metric == ORC_METRIC_AFFINE2P) {
+    /* wavefront_penalties_set_affine2p (wavefront/wavefront_penalties.c:132-173);
+     * wavefront_components_dimensions_affine2p (wavefront_components.c:97-116);
+     * wavefront_bialign_overlap_gopen_adjust (wavefront_bialign.c:396-410) */
+    if (match < 0) {
+      c->pen.x = 2 * x - 2 * match; c->pen.o = 2 * o; c->pen.e = 2 * e - match;
+      c->pen.o2 = 2 * o2; c->pen.e2 = 2 * e2 - match;
+    } else {
+      c->pen.x = x; c->pen.o = o; c->pen.e = e; c->pen.o2 = o2; c->pen.e2 = e2;
+    }
+    int sc = c->pen.x;
+    if (sc < c->pen.o + c->pen.e) sc = c->pen.o + c->pen.e;
+    if (sc < c->pen.o2 + c->pen.e2) sc = c->pen.o2 + c->pen.e2;
+    c->pen.scope = sc + 1;
+    c->pen.go_adj = c->pen.o > c->pen.o2 ? c->pen.o : c->pen.o2;
   } else {
     /* wavefront_penalties_set_affine (wavefront/wavefront_penalties.c:95-130) */
     if (match < 0) {
@@ -810,9 +968,10 @@ static void ctx_free(ctx_t* c) {
   free(c->rP); free(c->rT); free(c->leaf);
 }
 
-static int validate(int metric, int match, int x, int o, int e) {
+static int validate(int metric, int match, int x, int o, int e, int o2, int e2) {
   if (metric == ORC_METRIC_EDIT || metric == ORC_METRIC_INDEL) return 1;
   if (metric == ORC_METRIC_LINEAR) return !(match > 0 || x <= 0 || o <= 0);
+  if (metric == ORC_METRIC_AFFINE2P) return !(match > 0 || x <= 0 || o < 0 || e <= 0 || o2 < 0 || e2 <= 0);
   if (metric != ORC_METRIC_AFFINE) return 0;
   return !(match > 0 || x <= 0 || o < 0 || e <= 0);
 }
@@ -853,25 +1012,33 @@ static int align_one(ctx_t* c, const char* pattern, int plen, const char* text, 
     res->ops_len = score_only ? 0 : c->ops_len;
     if (score_only) res->score = c->cigar_score;
     else res->score = (c->ops_len > 0 && c->ops_len <= ops_cap)
-        ? rescore(c->pen.metric, ops, c->ops_len, c->match_orig, c->x_orig, c->o_orig, c->e_orig) : -1;
+        ? rescore(c->pen.metric, ops, c->ops_len, c->match_orig, c->x_orig, c->o_orig, c->e_orig, c->o2_orig,
+                  c->e2_orig)
+        : -1;
     res->n_cells = c->cnt.n_cells; res->n_ext = c->cnt.n_ext; res->n_steps = c->cnt.n_steps;
     res->max_leaf_score = c->cnt.max_leaf_score; res->max_depth = c->cnt.max_depth;
   }
   return final_status;
 }
 
-int orc_wfa_align(int metric, const char* pattern, int plen, const char* text, int tlen,
-                  int match, int mismatch, int gap_open, int gap_ext,
-                  int score_only, char* ops, int ops_cap, orc_result_t* res) {
-  if (!validate(metric, match, mismatch, gap_open, gap_ext) || plen < 0 || tlen < 0) {
+int orc_wfa_align_pen(int metric, const char* pattern, int plen, const char* text, int tlen, const int pen[6],
+                      int score_only, char* ops, int ops_cap, orc_result_t* res) {
+  if (!validate(metric, pen[0], pen[1], pen[2], pen[3], pen[4], pen[5]) || plen < 0 || tlen < 0) {
     if (res) { memset(res, 0, sizeof(*res)); res->status = ORC_STATUS_UNATTAINABLE; res->score = -1; }
     return ORC_STATUS_UNATTAINABLE;
   }
   ctx_t c;
-  ctx_init(&c, metric, match, mismatch, gap_open, gap_ext);
+  ctx_init(&c, metric, pen[0], pen[1], pen[2], pen[3], pen[4], pen[5]);
   const int st = align_one(&c, pattern, plen, text, tlen, score_only, ops, ops_cap, res);
   ctx_free(&c);
   return st;
+}
+
+int orc_wfa_align(int metric, const char* pattern, int plen, const char* text, int tlen,
+                  int match, int mismatch, int gap_open, int gap_ext,
+                  int score_only, char* ops, int ops_cap, orc_result_t* res) {
+  const int pen[6] = {match, mismatch, gap_open, gap_ext, 0, 1};
+  return orc_wfa_align_pen(metric, pattern, plen, text, tlen, pen, score_only, ops, ops_cap, res);
 }
 
 int orc_biwfa_align(const char* pattern, int plen, const char* text, int tlen,
@@ -886,7 +1053,7 @@ typedef struct {
   int tid, nthreads, n;
   const char* pat; const int64_t* pat_off; const int* plen;
   const char* txt; const int64_t* txt_off; const int* tlen;
-  int metric, match, x, o, e, score_only;
+  int metric, match, x, o, e, o2, e2, score_only;
   char* ops; const int64_t* ops_off;
   int* scores; int* status; int* ops_len;
 } job_t;
@@ -894,7 +1061,7 @@ typedef struct {
 static void* batch_worker(void* arg) {
   job_t* j = (job_t*)arg;
   ctx_t c;
-  ctx_init(&c, j->metric, j->match, j->x, j->o, j->e);
+  ctx_init(&c, j->metric, j->match, j->x, j->o, j->e, j->o2, j->e2);
   for (int i = j->tid; i < j->n; i += j->nthreads) {
     orc_result_t r;
     const int cap = j->plen[i] + j->tlen[i] + 1;
@@ -907,20 +1074,20 @@ static void* batch_worker(void* arg) {
   return NULL;
 }
 
-double orc_wfa_align_batch(int metric, int n, const char* pat, const int64_t* pat_off, const int* plen,
-                           const char* txt, const int64_t* txt_off, const int* tlen,
-                           int match, int mismatch, int gap_open, int gap_ext, int score_only,
-                           char* ops, const int64_t* ops_off,
-                           int* scores, int* status, int* ops_len, int nthreads) {
+double orc_wfa_align_batch_pen(int metric, int n, const char* pat, const int64_t* pat_off, const int* plen,
+                               const char* txt, const int64_t* txt_off, const int* tlen, const int pen[6],
+                               int score_only, char* ops, const int64_t* ops_off,
+                               int* scores, int* status, int* ops_len, int nthreads) {
   if (nthreads < 1) nthreads = 1;
-  if (!validate(metric, match, mismatch, gap_open, gap_ext)) return -1.0;
+  const int match = pen[0], mismatch = pen[1], gap_open = pen[2], gap_ext = pen[3], o2 = pen[4], e2 = pen[5];
+  if (!validate(metric, match, mismatch, gap_open, gap_ext, o2, e2)) return -1.0;
   pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
   job_t* jobs = (job_t*)malloc(sizeof(job_t) * (size_t)nthreads);
   struct timespec t0, t1;
   clock_gettime(CLOCK_MONOTONIC, &t0);
   for (int t = 0; t < nthreads; ++t) {
     job_t j = {t, nthreads, n, pat, pat_off, plen, txt, txt_off, tlen, metric, match, mismatch, gap_open, gap_ext,
-               score_only, ops, ops_off, scores, status, ops_len};
+               o2, e2, score_only, ops, ops_off, scores, status, ops_len};
     jobs[t] = j;
     pthread_create(&th[t], NULL, batch_worker, &jobs[t]);
   }
@@ -928,6 +1095,16 @@ double orc_wfa_align_batch(int metric, int n, const char* pat, const int64_t* pa
   clock_gettime(CLOCK_MONOTONIC, &t1);
   free(th); free(jobs);
   return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+double orc_wfa_align_batch(int metric, int n, const char* pat, const int64_t* pat_off, const int* plen,
+                           const char* txt, const int64_t* txt_off, const int* tlen,
+                           int match, int mismatch, int gap_open, int gap_ext, int score_only,
+                           char* ops, const int64_t* ops_off,
+                           int* scores, int* status, int* ops_len, int nthreads) {
+  const int pen[6] = {match, mismatch, gap_open, gap_ext, 0, 1};
+  return orc_wfa_align_batch_pen(metric, n, pat, pat_off, plen, txt, txt_off, tlen, pen, score_only, ops, ops_off,
+                                 scores, status, ops_len, nthreads);
 }
 
 double orc_biwfa_align_batch(int n, const char* pat, const int64_t* pat_off, const int* plen,

@@ -2,7 +2,8 @@
  * TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT.
  *
  * A plain-C restatement of WFA2-lib v2.3's bidirectional WFA (BiWFA) for the
- * gap-affine distance with match = 0 (or match < 0 through Eizenga's transform),
+ * gap-affine distance with match = 0 (or match < 0 through Eizenga's transform), and for
+ * the edit, indel, gap-linear and two-piece gap-affine distances,
  * end-to-end form, no heuristic, "ultralow" memory mode. Only tests/, the smoke
  * check and bench.py's CPU-baseline leg may load it, and only as the checker
  * or the timed CPU baseline. The GPU product never calls it.
@@ -36,6 +37,7 @@ extern "C" {
 #define ORC_METRIC_EDIT   1
 #define ORC_METRIC_INDEL  2
 #define ORC_METRIC_LINEAR 3
+#define ORC_METRIC_AFFINE2P 4  /* two-piece gap-affine: penalties (match, x, o1, e1, o2, e2) */
 
 typedef struct {
   int status;          /* final WFA2 status (0 = completed) */
@@ -62,6 +64,11 @@ int orc_wfa_align(int metric, const char* pattern, int plen, const char* text, i
                   int match, int mismatch, int gap_open, int gap_ext,
                   int score_only, char* ops, int ops_cap, orc_result_t* res);
 
+/* Any distance with the full penalty set pen = {match, mismatch, gap_open1, gap_ext1,
+ * gap_open2, gap_ext2} (the last two read by ORC_METRIC_AFFINE2P only). */
+int orc_wfa_align_pen(int metric, const char* pattern, int plen, const char* text, int tlen, const int pen[6],
+                      int score_only, char* ops, int ops_cap, orc_result_t* res);
+
 /* Align a batch with nthreads POSIX threads (static interleaved partition).
  * Sequences are concatenated: pattern i is pat[pat_off[i] .. pat_off[i]+plen[i]).
  * ops for pair i go to ops[ops_off[i] ..] (capacity plen+tlen+1 each).
@@ -77,6 +84,10 @@ double orc_wfa_align_batch(int metric, int n, const char* pat, const int64_t* pa
                            int match, int mismatch, int gap_open, int gap_ext, int score_only,
                            char* ops, const int64_t* ops_off,
                            int* scores, int* status, int* ops_len, int nthreads);
+double orc_wfa_align_batch_pen(int metric, int n, const char* pat, const int64_t* pat_off, const int* plen,
+                               const char* txt, const int64_t* txt_off, const int* tlen, const int pen[6],
+                               int score_only, char* ops, const int64_t* ops_off,
+                               int* scores, int* status, int* ops_len, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -113,3 +113,38 @@ int ref_wfa_align_gap_linear(const char* pattern, int plen, const char* text, in
   wavefront_aligner_delete(wf);
   return status;
 }
+
+/* The same for the two-piece gap-affine distance (penalties match, mismatch, o1, e1, o2, e2):
+ * *rescore_out is cigar_score_gap_affine2p() of the ops, as align_benchmark prints it. */
+int ref_wfa_align_affine2p(const char* pattern, int plen, const char* text, int tlen, const int pen6[6],
+                           int score_only, int* cigar_score_out, int* rescore_out, char* ops_out, int ops_cap,
+                           int* ops_len) {
+  wavefront_aligner_attr_t attr = wavefront_aligner_attr_default;
+  attr.distance_metric = gap_affine_2p;
+  attr.affine2p_penalties.match = pen6[0];
+  attr.affine2p_penalties.mismatch = pen6[1];
+  attr.affine2p_penalties.gap_opening1 = pen6[2];
+  attr.affine2p_penalties.gap_extension1 = pen6[3];
+  attr.affine2p_penalties.gap_opening2 = pen6[4];
+  attr.affine2p_penalties.gap_extension2 = pen6[5];
+  attr.memory_mode = wavefront_memory_ultralow;
+  attr.heuristic.strategy = wf_heuristic_none;
+  attr.alignment_scope = score_only ? compute_score : compute_alignment;
+  wavefront_aligner_t* const wf = wavefront_aligner_new(&attr);
+  const int status = wavefront_align(wf, pattern, plen, text, tlen);
+  cigar_t* const cigar = wf->cigar;
+  *cigar_score_out = cigar->score;
+  *ops_len = 0;
+  *rescore_out = -1;
+  if (!score_only && cigar->begin_offset < cigar->end_offset) {
+    const int n = cigar->end_offset - cigar->begin_offset;
+    if (n < ops_cap) {
+      memcpy(ops_out, cigar->operations + cigar->begin_offset, n);
+      ops_out[n] = '\0';
+      *ops_len = n;
+    }
+    *rescore_out = cigar_score_gap_affine2p(cigar, &attr.affine2p_penalties);
+  }
+  wavefront_aligner_delete(wf);
+  return status;
+}

@@ -4,12 +4,14 @@
    WFA2-lib/tests/: the 305 input pairs (wfa.utest.seq) and the expected `score\\tCIGAR`
    lines of the BiWFA gap-affine runs (test.biwfa.affine{,.p0..p5}.alg), the BiWFA
    score-only runs (test.biwfa.score.affine{,.p0..p5}.alg) and the BiWFA edit and indel
-   runs (test.biwfa{,.score}.{edit,indel}.alg). Penalties per file follow
-   WFA2-lib/tests/wfa.utest.sh:45-59; "metric" is 0 gap-affine, 1 edit, 2 indel.
+   runs (test.biwfa{,.score}.{edit,indel}.alg) and the BiWFA two-piece gap-affine runs
+   (test.biwfa{,.score}.affine2p.alg, align_benchmark's default penalties 0,4,6,2,24,1).
+   Penalties per file follow WFA2-lib/tests/wfa.utest.sh:45-59; "metric" is 0 gap-affine,
+   1 edit, 2 indel, 4 two-piece gap-affine.
 2. wfa2_ref_cases.json.gz — outputs of the real WFA2-lib v2.3 (oracle/_ref/libwfa2_ref.so,
    compiled from the reference sources by oracle/Makefile) on seeded synthetic pairs of
-   every workload and on edge cases, for the gap-affine, edit, indel and gap-linear distances
-   ("metric" 0, 1, 2, 3), so the GPU tests can pin parity on the GPU machine where the
+   every workload and on edge cases, for the gap-affine, edit, indel, gap-linear and two-piece
+   gap-affine distances ("metric" 0, 1, 2, 3, 4), so the GPU tests can pin parity on the GPU machine where the
    reference is absent.
 
 Usage:  python tests/golden/make_golden.py
@@ -52,6 +54,11 @@ LINEAR_SETS = {
     "test.biwfa.score.edit.alg": (1, True),
     "test.biwfa.score.indel.alg": (2, True),
 }
+AFFINE2P_SETS = {
+    # name: (penalties (match, mismatch, o1, e1, o2, e2), score_only)
+    "test.biwfa.affine2p.alg": ((0, 4, 6, 2, 24, 1), False),
+    "test.biwfa.score.affine2p.alg": ((0, 4, 6, 2, 24, 1), True),
+}
 
 
 def read_seq_file(path: Path):
@@ -72,6 +79,9 @@ def make_utest():
     for name, (metric, score_only) in LINEAR_SETS.items():
         lines = (WFA2_TESTS / "wfa.utest.check" / name).read_text().split("\n")[: len(pairs)]
         sets[name] = {"penalties": [0, 0, 0, 0], "score_only": score_only, "metric": metric, "lines": lines}
+    for name, (pen, score_only) in AFFINE2P_SETS.items():
+        lines = (WFA2_TESTS / "wfa.utest.check" / name).read_text().split("\n")[: len(pairs)]
+        sets[name] = {"penalties": list(pen), "score_only": score_only, "metric": 4, "lines": lines}
     out = {"source": "WFA2-lib/tests (v2.3)", "pairs": pairs, "sets": sets}
     with gzip.open(HERE / "wfa2_utest.json.gz", "wt") as f:
         json.dump(out, f)
@@ -145,6 +155,13 @@ def make_ref_cases():
         add(f"{tag}_generated", pen, False, gen(1, 8, 301) + gen(3, 12, 303), 3)
         add(f"{tag}_edges", pen, False, edges + far[:2], 3)
         add(f"{tag}_score_only", pen, True, gen(5, 24, 305), 3)
+    # two-piece gap-affine (match, mismatch, o1, e1, o2, e2), including match < 0 and a second
+    # piece cheaper to open than the first
+    for pen in ((0, 4, 6, 2, 24, 1), (0, 3, 4, 2, 12, 1), (-2, 3, 1, 2, 8, 1), (0, 4, 12, 1, 3, 4)):
+        tag = "affine2p_" + "_".join(map(str, pen))
+        add(f"{tag}_generated", pen, False, gen(1, 8, 401) + gen(3, 12, 403) + gen(2, 24, 402), 4)
+        add(f"{tag}_edges", pen, False, edges + far[:2], 4)
+        add(f"{tag}_score_only", pen, True, gen(5, 24, 405), 4)
     with gzip.open(HERE / "wfa2_ref_cases.json.gz", "wt") as f:
         json.dump({"source": "WFA2-lib v2.3 built from the reference sources (oracle/Makefile ref)",
                    "cases": cases}, f)

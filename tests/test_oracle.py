@@ -55,9 +55,13 @@ def test_oracle_matches_live_reference_on_random_pairs():
                 del t[pos:pos + int(rng.integers(1, 6))]
         t = "".join(t)
         pen = [(0, 4, 6, 2), (0, 1, 2, 1), (0, 5, 3, 2), (-3, 5, 3, 2)][trial % 4]
-        for metric in (binding.METRIC_AFFINE, binding.METRIC_EDIT, binding.METRIC_INDEL, binding.METRIC_LINEAR):
-            # gap-linear reads (match, mismatch, indel) from the first three penalties
+        for metric in (binding.METRIC_AFFINE, binding.METRIC_EDIT, binding.METRIC_INDEL, binding.METRIC_LINEAR,
+                       binding.METRIC_AFFINE2P):
+            # gap-linear reads (match, mismatch, indel) from the first three penalties; the
+            # two-piece distance adds a second gap piece (o2, e2) = (4*o1, max(e1 - 1, 1))
             mpen = (pen[0], pen[1], pen[3] + 1, 0) if metric == binding.METRIC_LINEAR else pen
+            if metric == binding.METRIC_AFFINE2P:
+                mpen = tuple(pen) + (4 * pen[2], max(pen[3] - 1, 1))
             ref = binding.ref_align(p, t, mpen, metric=metric)
             st, score, ops, _ = binding.oracle_align(p, t, mpen, metric=metric)
             assert (st, score, ops) == (ref[0], ref[1], ref[2]), (p, t, mpen, metric)
