@@ -26,7 +26,7 @@ ALIGNMENT_END2END, ALIGNMENT_ENDSFREE = 0, 1
 WF_HEURISTIC_NONE, WF_HEURISTIC_WFADAPTIVE = 0, 4
 WAVEFRONT_MEMORY_HIGH, WAVEFRONT_MEMORY_ULTRALOW = 0, 3
 SCHED_PLAIN, SCHED_LEARNED, SCHED_GIVEN, SCHED_SORTED = 0, 1, 2, 3
-METRIC_GAP_AFFINE, METRIC_EDIT, METRIC_INDEL, METRIC_GAP_LINEAR = 0, 1, 2, 3
+METRIC_GAP_AFFINE, METRIC_EDIT, METRIC_INDEL, METRIC_GAP_LINEAR, METRIC_GAP_AFFINE_2P = 0, 1, 2, 3, 4
 
 # SAM op codes of the output runs
 OP_INS, OP_DEL, OP_EQ, OP_X = 1, 2, 7, 8
@@ -95,7 +95,8 @@ class Aligner(C.Structure):
 
 class Config(C.Structure):
     _fields_ = [("match", C.c_int), ("mismatch", C.c_int), ("gap_opening", C.c_int), ("gap_extension", C.c_int),
-                ("score_only", C.c_int), ("max_alignment_steps", C.c_int), ("metric", C.c_int)]
+                ("score_only", C.c_int), ("max_alignment_steps", C.c_int), ("metric", C.c_int),
+                ("gap_opening2", C.c_int), ("gap_extension2", C.c_int)]
 
 
 class Stats(C.Structure):

@@ -158,9 +158,12 @@ class BatchAligner:
 
     @staticmethod
     def config(penalties=(0, 4, 6, 2), score_only=False, max_steps=0, metric=0) -> _capi.Config:
-        """metric: _capi.METRIC_GAP_AFFINE (default), METRIC_EDIT or METRIC_INDEL (penalties unused)."""
-        m, x, o, e = penalties
-        return _capi.Config(m, x, o, e, 1 if score_only else 0, max_steps, metric)
+        """metric: _capi.METRIC_GAP_AFFINE (default), METRIC_EDIT or METRIC_INDEL (penalties unused),
+        METRIC_GAP_LINEAR (match, mismatch, indel, -) or METRIC_GAP_AFFINE_2P (match, mismatch,
+        o1, e1, o2, e2)."""
+        m, x, o, e = penalties[:4]
+        o2, e2 = (penalties[4], penalties[5]) if len(penalties) >= 6 else (0, 0)
+        return _capi.Config(m, x, o, e, 1 if score_only else 0, max_steps, metric, o2, e2)
 
     def upload(self, b: PairBatch):
         self._batch = b  # keep host buffers alive

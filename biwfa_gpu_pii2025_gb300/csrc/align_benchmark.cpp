@@ -7,10 +7,11 @@
 //                       CIGAR is empty; score-only prints cigar->score and "-")
 //   --output-full PATH  "plen<TAB>tlen<TAB>score<TAB>pattern<TAB>text<TAB>CIGAR" (:118-142)
 // The score of a full alignment is the CIGAR rescored with the gap-affine penalties
-// (cigar_score_gap_affine), with the linear penalties for gap-linear-wfa
+// (cigar_score_gap_affine), with the two-piece penalties for gap-affine2p-wfa
+// (cigar_score_gap_affine2p), with the linear penalties for gap-linear-wfa
 // (cigar_score_gap_linear), or its number of edits for edit-wfa / indel-wfa
 // (cigar_score_edit), as align_benchmark prints it. Options follow align_benchmark_params.c;
-// configurations other than BiWFA without heuristics for those four distances are refused
+// configurations other than BiWFA without heuristics for those five distances are refused
 // with exit status 1, as align_benchmark refuses bad options.
 #include <chrono>
 #include <cstdio>
@@ -29,6 +30,7 @@ struct Options {
   bool output_full = false;
   int match = 0, mismatch = 4, gap_opening = 6, gap_extension = 2;
   int lin_match = 0, lin_mismatch = 4, lin_indel = 2;  // --linear-penalties (align_benchmark defaults)
+  int p2[6] = {0, 4, 6, 2, 24, 1};                     // --affine2p-penalties (align_benchmark defaults)
   bool score_only = false;
   std::string span = "global", memory = "ultralow", heuristic = "none";
   int max_steps = 0;
@@ -41,8 +43,9 @@ struct Options {
   if (msg) fprintf(stderr, "%s\n", msg);
   fprintf(stderr,
           "USE: align_benchmark -i PATH [-o PATH | --output-full PATH] [options]\n"
-          "      --algorithm|a gap-affine-wfa | gap-linear-wfa | edit-wfa | indel-wfa\n"
+          "      --algorithm|a gap-affine-wfa | gap-affine2p-wfa | gap-linear-wfa | edit-wfa | indel-wfa\n"
           "      --affine-penalties|g M,X,O,E          (default 0,4,6,2)\n"
+          "      --affine2p-penalties M,X,O1,E1,O2,E2  (default 0,4,6,2,24,1)\n"
           "      --linear-penalties|p M,X,I             (default 0,4,2)\n"
           "      --wfa-score-only\n"
           "      --wfa-span global   --wfa-memory ultralow   --wfa-heuristic none\n"
@@ -69,6 +72,10 @@ Options parse(int argc, char** argv) {
       const char* v = need_value(i, argc, argv);
       if (sscanf(v, "%d,%d,%d,%d", &o.match, &o.mismatch, &o.gap_opening, &o.gap_extension) != 4)
         usage_exit("--affine-penalties expects M,X,O,E");
+    } else if (a == "--affine2p-penalties") {
+      const char* v = need_value(i, argc, argv);
+      if (sscanf(v, "%d,%d,%d,%d,%d,%d", &o.p2[0], &o.p2[1], &o.p2[2], &o.p2[3], &o.p2[4], &o.p2[5]) != 6)
+        usage_exit("--affine2p-penalties expects M,X,O1,E1,O2,E2");
     } else if (a == "-p" || a == "--linear-penalties") {
       const char* v = need_value(i, argc, argv);
       if (sscanf(v, "%d,%d,%d", &o.lin_match, &o.lin_mismatch, &o.lin_indel) != 3)
@@ -84,9 +91,10 @@ Options parse(int argc, char** argv) {
     else if (a == "-h" || a == "--help") usage_exit(nullptr);
     else usage_exit((std::string("unknown option ") + a).c_str());
   }
-  if (o.algorithm != "gap-affine-wfa" && o.algorithm != "gap-linear-wfa" && o.algorithm != "edit-wfa" &&
-      o.algorithm != "indel-wfa")
-    usage_exit("only --algorithm gap-affine-wfa, gap-linear-wfa, edit-wfa or indel-wfa runs on the GPU aligner");
+  if (o.algorithm != "gap-affine-wfa" && o.algorithm != "gap-affine2p-wfa" && o.algorithm != "gap-linear-wfa" &&
+      o.algorithm != "edit-wfa" && o.algorithm != "indel-wfa")
+    usage_exit("only --algorithm gap-affine-wfa, gap-affine2p-wfa, gap-linear-wfa, edit-wfa or indel-wfa runs on "
+               "the GPU aligner");
   if (o.memory != "ultralow") usage_exit("only --wfa-memory ultralow (BiWFA) runs on the GPU aligner");
   if (o.heuristic != "none") usage_exit("only --wfa-heuristic none runs on the GPU aligner");
   if (o.span != "global") usage_exit("BiWFA aligns end-to-end only (--wfa-span global)");
@@ -145,9 +153,14 @@ int main(int argc, char** argv) {
   if (!ctx) { fprintf(stderr, "no usable CUDA device %d\n", opt.device); return 1; }
   const int metric = opt.algorithm == "edit-wfa" ? WFG_METRIC_EDIT
                    : opt.algorithm == "indel-wfa" ? WFG_METRIC_INDEL
-                   : opt.algorithm == "gap-linear-wfa" ? WFG_METRIC_GAP_LINEAR : WFG_METRIC_GAP_AFFINE;
+                   : opt.algorithm == "gap-linear-wfa" ? WFG_METRIC_GAP_LINEAR
+                   : opt.algorithm == "gap-affine2p-wfa" ? WFG_METRIC_GAP_AFFINE_2P : WFG_METRIC_GAP_AFFINE;
   wfg_config_t cfg{opt.match, opt.mismatch, opt.gap_opening, opt.gap_extension, opt.score_only ? 1 : 0,
-                   opt.max_steps, metric};
+                   opt.max_steps, metric, 0, 0};
+  if (metric == WFG_METRIC_GAP_AFFINE_2P) {
+    cfg.match = opt.p2[0]; cfg.mismatch = opt.p2[1]; cfg.gap_opening = opt.p2[2]; cfg.gap_extension = opt.p2[3];
+    cfg.gap_opening2 = opt.p2[4]; cfg.gap_extension2 = opt.p2[5];
+  }
   if (metric == WFG_METRIC_GAP_LINEAR) {
     cfg.match = opt.lin_match; cfg.mismatch = opt.lin_mismatch; cfg.gap_opening = opt.lin_indel; cfg.gap_extension = 0;
   }

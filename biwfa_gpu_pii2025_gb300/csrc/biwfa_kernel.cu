@@ -1,4 +1,5 @@
-// GB300 (sm_103a) bidirectional WFA, gap-affine, end-to-end: score + CIGAR on the device.
+// GB300 (sm_103a) bidirectional WFA, end-to-end: score + CIGAR on the device, for the
+// gap-affine distance and the edit, indel, gap-linear and two-piece gap-affine ones.
 //
 // A group of G warps (G = 1 for most pairs, 4 or 8 for wide ones) owns one pair at a time;
 // groups pull pair indices from a global work queue (one atomicAdd per pair) so a single
@@ -6,14 +7,16 @@
 // of every wavefront; all control state (scores, breakpoints, recursion) is group-uniform.
 //
 // Semantics follow WFA2-lib v2.3 exactly (paths relative to WFA2-lib/):
-//   compute      wavefront/wavefront_compute_affine.c:44-86, 229-260; wavefront_compute.c:40-104, 306-632
+//   compute      wavefront/wavefront_compute_affine.c:44-86, 229-260; wavefront_compute.c:40-104, 306-632;
+//                wavefront_compute_affine2p.c:44-104, 334-368; wavefront_compute_edit.c;
+//                wavefront_compute_linear.c
 //   extend       wavefront/wavefront_extend.c:86-211; wavefront_extend_kernels.c:68-152
 //   termination  wavefront/wavefront_termination.c:37-114
 //   breakpoint   wavefront/wavefront_bialign.c:189-519
 //   recursion    wavefront/wavefront_bialign.c:520-730
 //   leaf         wavefront/wavefront_bialign.c:155-185; wavefront_unialign.c:54-273
 //   backtrace    wavefront/wavefront_backtrace.c:41-219, 320-529
-//   rescoring    alignment/cigar.c:277-303
+//   rescoring    alignment/cigar.c:244-342
 #include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -40,11 +43,17 @@ constexpr int kMinBlocksPerSM = WFG_G1_MIN_BLOCKS;  // 7: caps registers at 72 s
 constexpr int kStepUnroll = WFG_STEP_UNROLL;        // diagonals per thread per step iteration (rings)
 constexpr int kLeafUnroll = WFG_LEAF_UNROLL;        // the same for the leaf store (narrower steps)
 constexpr int ST_OK = -1, ST_END_REACHED = -2, ST_END_UNREACHABLE = -3;
-constexpr int CM = 0, CI = 1, CD = 3;      // components (affine2p_matrix_type values)
+constexpr int CM = 0, CI = 1, CI2 = 2, CD = 3, CD2 = 4;  // components (affine2p_matrix_type values)
 constexpr int kFallbackMinScore = 250, kFallbackMinLength = 100, kRecoveryMinScore = 500;
-constexpr int BT_M = 9, BT_D_EXT = 6, BT_D_OPEN = 5, BT_I_EXT = 2, BT_I_OPEN = 1;
+constexpr int BT_M = 9, BT_D2_EXT = 8, BT_D2_OPEN = 7, BT_D_EXT = 6, BT_D_OPEN = 5, BT_I2_EXT = 4, BT_I2_OPEN = 3,
+              BT_I_EXT = 2, BT_I_OPEN = 1;
 
-__device__ __forceinline__ int comp_index(int c) { return c == CM ? 0 : (c == CI ? 1 : 2); }
+// Storage index of a component: M, I1, D1 (0-2, every gap distance), then the second gap
+// piece's I2, D2 (3-4, two-piece gap-affine only), kept in a separate region so that the
+// three-component layout does not change.
+__device__ __forceinline__ int comp_index(int c) {
+  return c == CM ? 0 : c == CI ? 1 : c == CD ? 2 : c == CI2 ? 3 : 4;
+}
 
 // A view of one stored wavefront. Offsets for diagonal k live at base[(k - kbase) & mask]:
 // rings use kbase = 0 and a power-of-two mask (circular over diagonals), the leaf store
@@ -67,11 +76,12 @@ __device__ __forceinline__ WfRef absent_ref() {
   return r;
 }
 
-// Internal penalties. metric: kMetricAffine, kMetricEdit, kMetricIndel or kMetricLinear (o =
-// indel, e = 0); go: the gap-opening adjust of the overlap and its stop conditions (o for
-// gap-affine, 0 otherwise, wavefront/wavefront_bialign.c:396-410).
-struct Pen { int x, o, e, scope, metric, go; };
-constexpr int kMetricAffine = 0, kMetricEdit = 1, kMetricIndel = 2, kMetricLinear = 3;
+// Internal penalties. metric: kMetricAffine, kMetricEdit, kMetricIndel, kMetricLinear (o =
+// indel, e = 0) or kMetricAffine2p (o, e the first gap piece, o2, e2 the second); go: the
+// gap-opening adjust of the overlap and its stop conditions (o for gap-affine, max(o, o2) for
+// two-piece gap-affine, 0 otherwise, wavefront/wavefront_bialign.c:396-410).
+struct Pen { int x, o, e, scope, metric, go, o2, e2; };
+constexpr int kMetricAffine = 0, kMetricEdit = 1, kMetricIndel = 2, kMetricLinear = 3, kMetricAffine2p = 4;
 
 // Oriented window over packed words (forward arrays for the forward aligner and the
 // leaf, reversed arrays for the reverse aligner). bshift = log2(bits per character).
@@ -182,10 +192,12 @@ struct DirCfg {
   int W;             // ring width (power of two)
   int nphys;         // physical ring buffers (round-robin over non-null steps)
   int lmax;          // leaf descriptor capacity (scores)
+  int nc;            // stored components: 3 (M, I1, D1) or 5 (+ I2, D2)
   int2* rdesc;       // ring descriptors [scope*3] (shared memory)
+  int2* rdesc2;      // I2/D2 ring descriptors [scope*2] (warp arena; nc == 5 only)
   int* rphys;        // physical buffer of each ring slot [scope] (shared memory)
-  int32_t* rdata;    // ring storage [nphys*3][W]
-  int4* ldesc;       // leaf descriptors [(lmax+1)*3] {lo, hi, data_off, kbase}
+  int32_t* rdata;    // ring storage [nphys*3][W], then I2/D2 [nphys*2][W] when nc == 5
+  int4* ldesc;       // leaf descriptors [(lmax+1)*3] {lo, hi, data_off, kbase}, then I2/D2 [(lmax+1)*2]
   int32_t* ldata;
 };
 
@@ -213,13 +225,14 @@ __device__ __forceinline__ WfRef ref_raw(const DirCfg& c, int score, int ci) {
   const bool leaf = MODE < 0 ? (c.leaf != 0) : (MODE == 1);
   if (!leaf) {
     const int slot = slot_of(c, score);
-    const int2 ds = c.rdesc[slot * 3 + ci];
+    const int2 ds = ci < 3 ? c.rdesc[slot * 3 + ci] : c.rdesc2[slot * 2 + (ci - 3)];
     r.lo = ds.x; r.hi = ds.y;
-    r.base = c.rdata + (size_t)(c.rphys[slot] * 3 + ci) * (size_t)c.W;
+    const int buf = ci < 3 ? c.rphys[slot] * 3 + ci : c.nphys * 3 + c.rphys[slot] * 2 + (ci - 3);
+    r.base = c.rdata + (size_t)buf * (size_t)c.W;
     r.kbase = 0; r.mask = (uint32_t)c.W - 1u;
   } else {
     if (score > c.lmax) return absent_ref();
-    const int4 ds = c.ldesc[score * 3 + ci];
+    const int4 ds = ci < 3 ? c.ldesc[score * 3 + ci] : c.ldesc[(c.lmax + 1) * 3 + score * 2 + (ci - 3)];
     r.lo = ds.x; r.hi = ds.y;
     r.base = c.ldata + ds.z;
     r.kbase = ds.w; r.mask = 0xffffffffu;
@@ -236,8 +249,13 @@ __device__ __forceinline__ WfRef fetch(const DirCfg& c, int score, int ci) {
 template <int MODE = -1>
 __device__ __forceinline__ void set_desc(const DirCfg& c, int score, int ci, int lo, int hi, int data_off, int kbase) {
   const bool leaf = MODE < 0 ? (c.leaf != 0) : (MODE == 1);
-  if (!leaf) c.rdesc[slot_of(c, score) * 3 + ci] = make_int2(lo, hi);
-  else c.ldesc[score * 3 + ci] = make_int4(lo, hi, data_off, kbase);
+  if (!leaf) {
+    if (ci < 3) c.rdesc[slot_of(c, score) * 3 + ci] = make_int2(lo, hi);
+    else c.rdesc2[slot_of(c, score) * 2 + (ci - 3)] = make_int2(lo, hi);
+  } else {
+    if (ci < 3) c.ldesc[score * 3 + ci] = make_int4(lo, hi, data_off, kbase);
+    else c.ldesc[(c.lmax + 1) * 3 + score * 2 + (ci - 3)] = make_int4(lo, hi, data_off, kbase);
+  }
 }
 
 // wavefront_aligner_init / init_wf (wavefront/wavefront_aligner.c:251-417). The caller
@@ -249,14 +267,16 @@ __device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
   const int cbi = comp_index(cb);
   if (!c.leaf) {
     for (int i = 0; i < c.scope * 3; ++i) c.rdesc[i] = make_int2(kAbsent, INT_MIN);
+    if (c.nc == 5) for (int i = 0; i < c.scope * 2; ++i) c.rdesc2[i] = make_int2(kAbsent, INT_MIN);
     for (int i = 0; i < c.scope; ++i) c.rphys[i] = 0;
-    c.rdesc[cbi] = make_int2(0, 0);
-    c.rdata[(size_t)cbi * c.W] = 0;  // diagonal 0 of score 0 (physical buffer 0)
+    set_desc<0>(c, 0, cbi, 0, 0, 0, 0);
+    // diagonal 0 of score 0 (physical buffer 0)
+    c.rdata[(size_t)(cbi < 3 ? cbi : c.nphys * 3 + (cbi - 3)) * c.W] = 0;
     d.next_phys = 1 % c.nphys;
   } else {
     d.lused = 1;
-    for (int ci = 0; ci < 3; ++ci) c.ldesc[ci] = make_int4(kAbsent, INT_MIN, 0, 0);
-    c.ldesc[cbi] = make_int4(0, 0, 0, 0);
+    for (int ci = 0; ci < c.nc; ++ci) set_desc<1>(c, 0, ci, kAbsent, INT_MIN, 0, 0);
+    set_desc<1>(c, 0, cbi, 0, 0, 0, 0);
     c.ldata[0] = 0;
   }
 }
@@ -399,9 +419,143 @@ __device__ __noinline__ int dir_step_linear(Dir& d, const Pen p, int s, const Gr
   return 0;
 }
 
+// The two-piece gap-affine step: wavefront_compute_affine2p (wavefront/wavefront_compute_affine2p.c:
+// 334-368) with the idm kernel (:44-104), then extension and termination as in dir_step.
+// Seven inputs (M[s-x], M[s-o1-e1], I1/D1[s-e1], M[s-o2-e2], I2/D2[s-e2]); the output range
+// covers all of them; I1/D1/I2/D2 outputs exist when one of their inputs does
+// (wavefront_compute_allocate_output, wavefront/wavefront_compute.c:450-494). One diagonal
+// per thread per iteration: the nine input reads already keep enough loads in flight.
+template <int G, int MODE>
+__device__ __noinline__ int dir_step_2p(Dir& d, const Pen p, int s, const Grp<G> g, int* max_ak_out) {
+  const DirCfg c = d.cfg;
+  constexpr bool kLeaf = MODE == 1;
+  const int nn = d.num_null, used = d.lused, nphys = d.next_phys, ce = d.ce;
+  const SeqView sv = d.sv;
+  const uint32_t tl = (uint32_t)sv.tlen, pl = (uint32_t)sv.plen;
+  *max_ak_out = 0;
+  if (kLeaf && s > c.lmax) return -1;
+  const WfRef mx = fetch<MODE>(c, s - p.x, 0);
+  const WfRef mo1 = fetch<MODE>(c, s - p.o - p.e, 0);
+  const WfRef ie1 = fetch<MODE>(c, s - p.e, 1);
+  const WfRef de1 = fetch<MODE>(c, s - p.e, 2);
+  const WfRef mo2 = fetch<MODE>(c, s - p.o2 - p.e2, 0);
+  const WfRef ie2 = fetch<MODE>(c, s - p.e2, 3);
+  const WfRef de2 = fetch<MODE>(c, s - p.e2, 4);
+  const bool hx = mx.nonnull(), ho1 = mo1.nonnull(), hie1 = ie1.nonnull(), hde1 = de1.nonnull();
+  const bool ho2 = mo2.nonnull(), hie2 = ie2.nonnull(), hde2 = de2.nonnull();
+  if (!hx && !ho1 && !hie1 && !hde1 && !ho2 && !hie2 && !hde2) {
+    if (G > 1) g.sync();
+    d.num_null = nn + 1;
+    #pragma unroll
+    for (int ci = 0; ci < 5; ++ci) set_desc<MODE>(c, s, ci, kAbsent, INT_MIN, 0, 0);
+    if (nn + 1 > c.scope) { d.status = ST_END_UNREACHABLE; d.status_score = s; return 1; }
+    return 0;
+  }
+  // wavefront_compute_limits_input over the seven inputs
+  int lo = hx ? mx.lo : 1, hi = hx ? mx.hi : -1;
+  lo = min(lo, (ho1 ? mo1.lo : 1) - 1);   hi = max(hi, (ho1 ? mo1.hi : -1) + 1);
+  lo = min(lo, (hie1 ? ie1.lo : 1) + 1);  hi = max(hi, (hie1 ? ie1.hi : -1) + 1);
+  lo = min(lo, (hde1 ? de1.lo : 1) - 1);  hi = max(hi, (hde1 ? de1.hi : -1) - 1);
+  lo = min(lo, (ho2 ? mo2.lo : 1) - 1);   hi = max(hi, (ho2 ? mo2.hi : -1) + 1);
+  lo = min(lo, (hie2 ? ie2.lo : 1) + 1);  hi = max(hi, (hie2 ? ie2.hi : -1) + 1);
+  lo = min(lo, (hde2 ? de2.lo : 1) - 1);  hi = max(hi, (hde2 ? de2.hi : -1) - 1);
+  const bool ai1 = ho1 || hie1, ad1 = ho1 || hde1, ai2 = ho2 || hie2, ad2 = ho2 || hde2;
+  const int width = hi - lo + 1;
+  WfRef om, oi1, od1, oi2, od2;
+  int offm = 0, offi1 = 0, offd1 = 0, offi2 = 0, offd2 = 0, need = 0;
+  if (!kLeaf) {
+    if (width > c.W) return -1;
+    om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
+    oi1.base = om.base + c.W;
+    od1.base = oi1.base + c.W;
+    oi2.base = c.rdata + (size_t)(c.nphys * 3 + nphys * 2) * c.W;
+    od2.base = oi2.base + c.W;
+    om.kbase = oi1.kbase = od1.kbase = oi2.kbase = od2.kbase = 0;
+    om.mask = oi1.mask = od1.mask = oi2.mask = od2.mask = (uint32_t)c.W - 1u;
+  } else {
+    need = width * (1 + (ai1 ? 1 : 0) + (ad1 ? 1 : 0) + (ai2 ? 1 : 0) + (ad2 ? 1 : 0));
+    if (used + need > d.lcap) return -1;
+    offm = used;
+    offi1 = offm + width;
+    offd1 = offi1 + (ai1 ? width : 0);
+    offi2 = offd1 + (ad1 ? width : 0);
+    offd2 = offi2 + (ai2 ? width : 0);
+    om.base = c.ldata + offm; oi1.base = c.ldata + offi1; od1.base = c.ldata + offd1;
+    oi2.base = c.ldata + offi2; od2.base = c.ldata + offd2;
+    om.kbase = oi1.kbase = od1.kbase = oi2.kbase = od2.kbase = lo;
+    om.mask = oi1.mask = od1.mask = oi2.mask = od2.mask = 0xffffffffu;
+  }
+  // ra: M, I1, D1 trimmed lo/hi; rb: I2, D2 trimmed lo/hi, then the max antidiagonal of the
+  // extended M (two reductions of at most 8 values each)
+  int ra[6] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};
+  int rb[5] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, 0};
+  for (int k = lo + g.tid; k <= hi; k += 32 * G) {
+    const int32_t i1 = max(mo1.get(k - 1), ie1.get(k - 1)) + 1;
+    const int32_t i2 = max(mo2.get(k - 1), ie2.get(k - 1)) + 1;
+    const int32_t d1 = max(mo1.get(k + 1), de1.get(k + 1));
+    const int32_t d2 = max(mo2.get(k + 1), de2.get(k + 1));
+    int32_t m = max(max(mx.get(k) + 1, max(i1, i2)), max(d1, d2));
+    if ((uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
+    if (m != kNull) {
+      ra[0] = min(ra[0], k); ra[1] = max(ra[1], k);
+      m += lcp(sv, m - k, m);
+      rb[4] = max(rb[4], 2 * m - k);
+    }
+    om.put(k, m);
+    if (ai1) {
+      oi1.put(k, i1);
+      if ((uint32_t)i1 <= tl && (uint32_t)(i1 - k) <= pl) { ra[2] = min(ra[2], k); ra[3] = max(ra[3], k); }
+    }
+    if (ad1) {
+      od1.put(k, d1);
+      if ((uint32_t)d1 <= tl && (uint32_t)(d1 - k) <= pl) { ra[4] = min(ra[4], k); ra[5] = max(ra[5], k); }
+    }
+    if (ai2) {
+      oi2.put(k, i2);
+      if ((uint32_t)i2 <= tl && (uint32_t)(i2 - k) <= pl) { rb[0] = min(rb[0], k); rb[1] = max(rb[1], k); }
+    }
+    if (ad2) {
+      od2.put(k, d2);
+      if ((uint32_t)d2 <= tl && (uint32_t)(d2 - k) <= pl) { rb[2] = min(rb[2], k); rb[3] = max(rb[3], k); }
+    }
+  }
+  const bool ma[6] = {false, true, false, true, false, true};
+  const bool mb[5] = {false, true, false, true, true};
+  g.minmax(ra, ma);
+  g.minmax(rb, mb);
+  g.sync();
+  d.num_null = 0;
+  if (kLeaf) d.lused = used + need;
+  else { c.rphys[slot_of(c, s)] = nphys; d.next_phys = (nphys + 1 == c.nphys) ? 0 : nphys + 1; }
+  if (ra[0] <= ra[1]) set_desc<MODE>(c, s, 0, ra[0], ra[1], offm, lo); else set_desc<MODE>(c, s, 0, lo, lo - 1, offm, lo);
+  const bool alloc[4] = {ai1, ad1, ai2, ad2};
+  const int tlo[4] = {ra[2], ra[4], rb[0], rb[2]}, thi[4] = {ra[3], ra[5], rb[1], rb[3]};
+  const int toff[4] = {offi1, offd1, offi2, offd2};
+  #pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (!alloc[j]) set_desc<MODE>(c, s, j + 1, kAbsent, INT_MIN, 0, 0);
+    else if (tlo[j] <= thi[j]) set_desc<MODE>(c, s, j + 1, tlo[j], thi[j], toff[j], lo);
+    else set_desc<MODE>(c, s, j + 1, lo, lo - 1, toff[j], lo);
+  }
+  // wavefront_termination_end2end on component_end at score s
+  const int ak = sv.tlen - sv.plen;
+  bool done;
+  if (ce == CM) {
+    done = (ra[0] <= ak && ak <= ra[1]) && (om.at(ak) >= sv.tlen);
+  } else {
+    const int j = (ce == CI) ? 0 : (ce == CD) ? 1 : (ce == CI2) ? 2 : 3;
+    const WfRef& t = (j == 0) ? oi1 : (j == 1) ? od1 : (j == 2) ? oi2 : od2;
+    done = alloc[j] && (tlo[j] <= ak && ak <= thi[j]) && (t.at(ak) >= sv.tlen);
+  }
+  if (done) { d.status = ST_END_REACHED; d.status_score = s; d.end_k = ak; return 1; }
+  *max_ak_out = rb[4];
+  return 0;
+}
+
 template <int G, int MODE>
 __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g, int* max_ak_out) {
   if (p.metric == kMetricEdit || p.metric == kMetricIndel) return dir_step_linear<G, MODE>(d, p, s, g, max_ak_out);
+  if (p.metric == kMetricAffine2p) return dir_step_2p<G, MODE>(d, p, s, g, max_ak_out);
   const DirCfg c = d.cfg;
   constexpr bool kLeaf = MODE == 1;  // the leaf store (else the modular rings)
   // gap-linear (wavefront_compute_linear, wavefront/wavefront_compute_linear.c:166-195): the
@@ -577,7 +731,8 @@ __device__ void bp_scan(bool is_m, bool fwd, int s0, int s1, const WfRef& w0, co
   }
 }
 
-// wavefront_bialign_overlap (gap-affine part)
+// wavefront_bialign_overlap (wavefront/wavefront_bialign.c:314-392): for two-piece
+// gap-affine the I2/D2 pairs first (gap-open o2), then I1/D1 (o1), then M.
 template <int G>
 __device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s1, bool fwd, BP& bp, const Pen p,
                                      const Grp<G> g) {
@@ -587,10 +742,18 @@ __device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s
   if (!m0.present()) return;
   const WfRef dd0 = ref_raw<0>(c0, s0, 2);
   const WfRef ii0 = ref_raw<0>(c0, s0, 1);
+  const bool two = p.metric == kMetricAffine2p;
   for (int i = 0; i < p.scope; ++i) {
     const int si = s1 - i;
     if (si < 0) break;
-    if (s0 + si - p.go >= bp.score) continue;
+    if (two) {
+      if (s0 + si - p.o2 >= bp.score) continue;
+      const WfRef dd20 = ref_raw<0>(c0, s0, 4), dd21 = ref_raw<0>(c1, si, 4);
+      if (dd20.present() && dd21.present()) bp_scan<G>(false, fwd, s0, si, dd20, dd21, plen, tlen, p.o2, CD2, bp, g);
+      const WfRef ii20 = ref_raw<0>(c0, s0, 3), ii21 = ref_raw<0>(c1, si, 3);
+      if (ii20.present() && ii21.present()) bp_scan<G>(false, fwd, s0, si, ii20, ii21, plen, tlen, p.o2, CI2, bp, g);
+    }
+    if (s0 + si - (two ? p.o : p.go) >= bp.score) continue;
     const WfRef dd1 = ref_raw<0>(c1, si, 2);
     if (dd0.present() && dd1.present()) bp_scan<G>(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, g);
     const WfRef ii1 = ref_raw<0>(c1, si, 1);
@@ -746,7 +909,8 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
     if (rlen > 0) { if (nrev < lruns_cap) lruns[nrev] = ((uint32_t)rlen << 4) | (uint32_t)rop; else rover = true; ++nrev; }
     rop = op; rlen = len;
   };
-  const bool lin = p.metric != kMetricAffine;
+  const bool lin = p.metric != kMetricAffine && p.metric != kMetricAffine2p;
+  const bool two = p.metric == kMetricAffine2p;
   int matrix = ce, score = s, k = B.end_k;
   int32_t off = tlen;
   int h = off, v = off - k;
@@ -761,6 +925,7 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
     // (wavefront/wavefront_backtrace.c:223-319): M sources only, gap-open = o, no mismatch
     // source for indel
     const int mm = score - p.x, go = score - p.o - (lin ? 0 : p.e), ge = score - p.e;
+    const int go2 = score - p.o2 - p.e2, ge2 = score - p.e2;  // second gap piece (two-piece only)
     long long max_all;
     if (matrix == CM) {
       const long long mis = (p.metric == kMetricIndel) ? (long long)kNull : bt_src(bc, mm, 0, k, 1, BT_M);
@@ -768,17 +933,35 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
       const long long ix = lin ? (long long)kNull : bt_src(bc, ge, 1, k - 1, 1, BT_I_EXT);
       const long long dop = bt_src(bc, go, 0, k + 1, 0, BT_D_OPEN);
       const long long dx = lin ? (long long)kNull : bt_src(bc, ge, 2, k + 1, 0, BT_D_EXT);
-      const long long mi = io >= ix ? io : ix;
-      const long long md = dop >= dx ? dop : dx;
+      long long mi = io >= ix ? io : ix;
+      long long md = dop >= dx ? dop : dx;
+      if (two) {
+        const long long io2 = bt_src(bc, go2, 0, k - 1, 1, BT_I2_OPEN);
+        const long long ix2 = bt_src(bc, ge2, 3, k - 1, 1, BT_I2_EXT);
+        const long long dop2 = bt_src(bc, go2, 0, k + 1, 0, BT_D2_OPEN);
+        const long long dx2 = bt_src(bc, ge2, 4, k + 1, 0, BT_D2_EXT);
+        const long long mi2 = io2 >= ix2 ? io2 : ix2;
+        const long long md2 = dop2 >= dx2 ? dop2 : dx2;
+        mi = mi >= mi2 ? mi : mi2;
+        md = md >= md2 ? md : md2;
+      }
       const long long mid = mi >= md ? mi : md;
       max_all = mis >= mid ? mis : mid;
     } else if (matrix == CI) {
       const long long io = bt_src(bc, go, 0, k - 1, 1, BT_I_OPEN);
       const long long ix = bt_src(bc, ge, 1, k - 1, 1, BT_I_EXT);
       max_all = io >= ix ? io : ix;
-    } else {
+    } else if (matrix == CD) {
       const long long dop = bt_src(bc, go, 0, k + 1, 0, BT_D_OPEN);
       const long long dx = bt_src(bc, ge, 2, k + 1, 0, BT_D_EXT);
+      max_all = dop >= dx ? dop : dx;
+    } else if (matrix == CI2) {
+      const long long io = bt_src(bc, go2, 0, k - 1, 1, BT_I2_OPEN);
+      const long long ix = bt_src(bc, ge2, 3, k - 1, 1, BT_I2_EXT);
+      max_all = io >= ix ? io : ix;
+    } else {
+      const long long dop = bt_src(bc, go2, 0, k + 1, 0, BT_D2_OPEN);
+      const long long dx = bt_src(bc, ge2, 4, k + 1, 0, BT_D2_EXT);
       max_all = dop >= dx ? dop : dx;
     }
     if (max_all < 0) break;
@@ -794,7 +977,11 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
     else if (type == BT_I_OPEN) { score = go; matrix = CM; push(WFG_OP_INS, 1); --k; --off; }
     else if (type == BT_I_EXT) { score = ge; matrix = CI; push(WFG_OP_INS, 1); --k; --off; }
     else if (type == BT_D_OPEN) { score = go; matrix = CM; push(WFG_OP_DEL, 1); ++k; }
-    else { score = ge; matrix = CD; push(WFG_OP_DEL, 1); ++k; }
+    else if (type == BT_D_EXT) { score = ge; matrix = CD; push(WFG_OP_DEL, 1); ++k; }
+    else if (type == BT_I2_OPEN) { score = go2; matrix = CM; push(WFG_OP_INS, 1); --k; --off; }
+    else if (type == BT_I2_EXT) { score = ge2; matrix = CI2; push(WFG_OP_INS, 1); --k; --off; }
+    else if (type == BT_D2_OPEN) { score = go2; matrix = CM; push(WFG_OP_DEL, 1); ++k; }
+    else { score = ge2; matrix = CD2; push(WFG_OP_DEL, 1); ++k; }
     v = off - k; h = off;
   }
   if (matrix == CM) {
@@ -817,9 +1004,12 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
   return ST_OK;
 }
 
-// cigar_score_gap_affine (alignment/cigar.c:277-303), cigar_score_gap_linear (:260-276; o is
-// the indel penalty), or cigar_score_edit (:244-259) for the edit and indel distances.
-__device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int metric, int match, int x, int o, int e) {
+// cigar_score_gap_affine (alignment/cigar.c:277-303), cigar_score_gap_affine2p (:304-342: per
+// gap run the cheaper piece), cigar_score_gap_linear (:260-276; o is the indel penalty), or
+// cigar_score_edit (:244-259) for the edit and indel distances. The runs are maximal (adjacent
+// runs of one op are merged when emitted).
+__device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int metric, int match, int x, int o, int e,
+                                            int o2, int e2) {
   int score = 0;
   for (int i = 0; i < n; ++i) {
     const int op = (int)(runs[i] & 15u), len = (int)(runs[i] >> 4);
@@ -827,6 +1017,7 @@ __device__ __forceinline__ int rescore_runs(const uint32_t* runs, int n, int met
     if (metric == kMetricLinear) { score -= (op == WFG_OP_EQ ? match : op == WFG_OP_X ? x : o) * len; continue; }
     if (op == WFG_OP_EQ) score -= match * len;
     else if (op == WFG_OP_X) score -= x * len;
+    else if (metric == kMetricAffine2p) score -= min(o + e * len, o2 + e2 * len);
     else score -= o + e * len;
   }
   return score;
@@ -864,10 +1055,11 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
   g.red = S.red;
   const long long ggroup = (long long)blockIdx.x * GROUPS + gib;
   const int nphys = P.ring_nphys > 0 ? P.ring_nphys : P.scope;
+  const int nc = P.metric == kMetricAffine2p ? 5 : 3;
   const ArenaLayout L = wfg_arena_layout(RING_SMEM ? 0 : nphys, P.ring_w, P.leaf_max_score, P.leaf_words,
-                                         P.run_cap, P.leaf_run_cap, P.stack_cap);
+                                         P.run_cap, P.leaf_run_cap, P.stack_cap, nc);
   uint8_t* arena = P.arena + ggroup * P.arena_bytes;
-  const size_t ring_dir = (size_t)nphys * 3 * P.ring_w;
+  const size_t ring_dir = (size_t)nphys * nc * P.ring_w;
   int32_t* ring = RING_SMEM ? s_ring_dyn + (size_t)gib * 2 * ring_dir : (int32_t*)(arena + L.ring_off);
   int4* ldesc = (int4*)(arena + L.ldesc_off);
   int32_t* ldata = (int32_t*)(arena + L.ldata_off);
@@ -880,18 +1072,21 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
   Dir& B = S.dir[2];
   const uint32_t magic = (uint32_t)(0xffffffffu / (uint32_t)P.scope) + 1u;
   DirCfg fc{};
-  fc.leaf = 0; fc.scope = P.scope; fc.magic = magic; fc.W = P.ring_w; fc.nphys = nphys; fc.lmax = 0;
-  fc.rdesc = S.rdesc[0]; fc.rphys = S.rphys[0]; fc.rdata = ring;
+  int2* rdesc2 = (int2*)(arena + L.rdesc2_off);  // I2/D2 ring descriptors of both directions
+  fc.leaf = 0; fc.scope = P.scope; fc.magic = magic; fc.W = P.ring_w; fc.nphys = nphys; fc.lmax = 0; fc.nc = nc;
+  fc.rdesc = S.rdesc[0]; fc.rdesc2 = rdesc2; fc.rphys = S.rphys[0]; fc.rdata = ring;
   DirCfg rc = fc;
-  rc.rdesc = S.rdesc[1]; rc.rphys = S.rphys[1]; rc.rdata = ring + ring_dir;
+  rc.rdesc = S.rdesc[1]; rc.rdesc2 = rdesc2 + kMaxScope * 2; rc.rphys = S.rphys[1]; rc.rdata = ring + ring_dir;
   DirCfg bcfg{};
   bcfg.leaf = 1; bcfg.scope = P.scope; bcfg.magic = magic; bcfg.W = 0; bcfg.nphys = 1; bcfg.lmax = P.leaf_max_score;
+  bcfg.nc = nc;
   bcfg.ldesc = ldesc; bcfg.ldata = ldata;
   F.cfg = fc; R.cfg = rc; B.cfg = bcfg;
   F.lcap = R.lcap = 0; F.lused = R.lused = 0;
   B.lcap = P.leaf_words; B.lused = 0;
   g.sync();
-  const Pen pen = {P.x, P.o, P.e, P.scope, P.metric, P.metric == kMetricAffine ? P.o : 0};
+  const int go = P.metric == kMetricAffine ? P.o : P.metric == kMetricAffine2p ? max(P.o, P.o2) : 0;
+  const Pen pen = {P.x, P.o, P.e, P.scope, P.metric, go, P.o2, P.e2};
 
   const unsigned long long num_pairs =
       P.num_pairs_ptr ? *P.num_pairs_ptr : (unsigned long long)P.num_pairs;
@@ -984,7 +1179,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
       if (status == ST_OK) status = WFG_ST_COMPLETED;
       g.sync();
       if (status == WFG_ST_COMPLETED) {
-        score = (out.n > 0) ? rescore_runs(runs, out.n, P.metric, P.match_o, P.x_o, P.o_o, P.e_o) : 0;
+        score = (out.n > 0) ? rescore_runs(runs, out.n, P.metric, P.match_o, P.x_o, P.o_o, P.e_o, P.o2_o, P.e2_o) : 0;
         int base_lo = 0, base_hi = 0;
         if (g.tid == 0) {
           const unsigned long long b = atomicAdd(P.out_head, (unsigned long long)out.n);
@@ -1074,7 +1269,8 @@ namespace {
 // Execution shapes: (warps per pair, groups per block, rings in shared memory).
 template <int G, int GROUPS, bool RS, int MINB>
 cudaError_t launch_shape(const KernelParams& p, int grid, cudaStream_t stream) {
-  const size_t dyn = RS ? (size_t)GROUPS * 2 * (size_t)(p.ring_nphys > 0 ? p.ring_nphys : p.scope) * 3 *
+  const size_t nc = p.metric == kMetricAffine2p ? 5 : 3;
+  const size_t dyn = RS ? (size_t)GROUPS * 2 * (size_t)(p.ring_nphys > 0 ? p.ring_nphys : p.scope) * nc *
                               (size_t)p.ring_w * sizeof(int32_t)
                         : 0;
   if (dyn > 0) {

@@ -38,8 +38,15 @@ void check_config(AlignerImpl* im) {
   const affine_penalties_t& p = a.affine_penalties;
   im->unsupported = 1;
   if (a.distance_metric != gap_affine && a.distance_metric != edit && a.distance_metric != indel &&
-      a.distance_metric != gap_linear) {
-    im->reason = "the two-piece affine distance is not supported"; return;
+      a.distance_metric != gap_linear && a.distance_metric != gap_affine_2p) {
+    im->reason = "unknown distance metric"; return;
+  }
+  const affine2p_penalties_t& q = a.affine2p_penalties;
+  if (a.distance_metric == gap_affine_2p &&
+      (q.match > 0 || q.mismatch <= 0 || q.gap_opening1 < 0 || q.gap_extension1 <= 0 || q.gap_opening2 < 0 ||
+       q.gap_extension2 <= 0)) {
+    im->reason = "two-piece penalties must satisfy match <= 0, mismatch > 0, o1 >= 0, e1 > 0, o2 >= 0, e2 > 0";
+    return;
   }
   if (a.distance_metric == gap_linear && (a.linear_penalties.match > 0 || a.linear_penalties.mismatch <= 0 ||
                                           a.linear_penalties.indel <= 0)) {
@@ -62,7 +69,7 @@ void check_config(AlignerImpl* im) {
 }
 
 wfg_config_t config_of(const AlignerImpl* im) {
-  wfg_config_t c;
+  wfg_config_t c{};
   c.match = im->attr.affine_penalties.match;
   c.mismatch = im->attr.affine_penalties.mismatch;
   c.gap_opening = im->attr.affine_penalties.gap_opening;
@@ -71,12 +78,19 @@ wfg_config_t config_of(const AlignerImpl* im) {
   c.max_alignment_steps = im->attr.system.max_alignment_steps;
   c.metric = (im->attr.distance_metric == edit) ? WFG_METRIC_EDIT
            : (im->attr.distance_metric == indel) ? WFG_METRIC_INDEL
-           : (im->attr.distance_metric == gap_linear) ? WFG_METRIC_GAP_LINEAR : WFG_METRIC_GAP_AFFINE;
+           : (im->attr.distance_metric == gap_linear) ? WFG_METRIC_GAP_LINEAR
+           : (im->attr.distance_metric == gap_affine_2p) ? WFG_METRIC_GAP_AFFINE_2P : WFG_METRIC_GAP_AFFINE;
   if (c.metric == WFG_METRIC_GAP_LINEAR) {
     c.match = im->attr.linear_penalties.match;
     c.mismatch = im->attr.linear_penalties.mismatch;
     c.gap_opening = im->attr.linear_penalties.indel;
     c.gap_extension = 0;
+  }
+  if (c.metric == WFG_METRIC_GAP_AFFINE_2P) {
+    const affine2p_penalties_t& q = im->attr.affine2p_penalties;
+    c.match = q.match; c.mismatch = q.mismatch;
+    c.gap_opening = q.gap_opening1; c.gap_extension = q.gap_extension1;
+    c.gap_opening2 = q.gap_opening2; c.gap_extension2 = q.gap_extension2;
   }
   return c;
 }

@@ -47,8 +47,11 @@ struct PairDesc {
 struct KernelParams {
   // penalties: internal (transformed when match < 0) and the caller's for rescoring
   int x, o, e, scope;
+  int o2, e2;                // second gap piece (two-piece gap-affine), internal
   int match_o, x_o, o_o, e_o;
-  int metric;                // 0 gap-affine, 1 edit, 2 indel (x, o, e, scope already set for it)
+  int o2_o, e2_o;            // second gap piece as the caller gave it
+  int metric;                // 0 gap-affine, 1 edit, 2 indel, 3 gap-linear, 4 two-piece gap-affine
+                             // (x, o, e, scope already set for it)
   int score_only;
   int max_steps;
   // pairs
@@ -93,30 +96,41 @@ WFG_HD constexpr inline int wfg_gcd(int a, int b) { return b == 0 ? a : wfg_gcd(
 WFG_HD constexpr inline int wfg_ring_buffers(int x, int o, int e) {
   return ((o + e > x ? o + e : x) + 1 + wfg_gcd(wfg_gcd(x, o + e), e) - 1) / wfg_gcd(wfg_gcd(x, o + e), e);
 }
+// The same for two gap pieces: g = gcd(x, o1+e1, e1, o2+e2, e2) over scope = max(x, o1+e1,
+// o2+e2) + 1.
+WFG_HD constexpr inline int wfg_ring_buffers_2p(int x, int o1, int e1, int o2, int e2) {
+  return ((o1 + e1 > x ? (o1 + e1 > o2 + e2 ? o1 + e1 : o2 + e2) : (x > o2 + e2 ? x : o2 + e2)) + 1 +
+          wfg_gcd(wfg_gcd(wfg_gcd(x, o1 + e1), wfg_gcd(e1, o2 + e2)), e2) - 1) /
+         wfg_gcd(wfg_gcd(wfg_gcd(x, o1 + e1), wfg_gcd(e1, o2 + e2)), e2);
+}
 
 // Per-warp arena carving (bytes); all offsets 256-byte aligned.
 struct ArenaLayout {
-  int64_t ring_off, ring_bytes;     // 2 directions x buffers x 3 components x ring_w int32
-  int64_t ldesc_off, ldesc_bytes;   // (leaf_max_score+1) x 3 x int4
+  int64_t ring_off, ring_bytes;     // 2 directions x buffers x ncomp components x ring_w int32
+  int64_t ldesc_off, ldesc_bytes;   // (leaf_max_score+1) x ncomp x int4
   int64_t ldata_off, ldata_bytes;   // leaf_words int32
   int64_t runs_off, runs_bytes;     // run_cap uint32
   int64_t lruns_off, lruns_bytes;   // leaf_run_cap uint32
   int64_t stack_off, stack_bytes;   // stack_cap x 8 int32
+  int64_t rdesc2_off, rdesc2_bytes; // I2/D2 ring descriptors, 2 directions x 32 scores x 2 x int2
+                                    // (ncomp == 5 only)
   int64_t total;
 };
 
 WFG_HD constexpr inline int64_t wfg_align256(int64_t v) { return (v + 255) & ~(int64_t)255; }
 
+// ncomp: 3 (M, I1, D1) or 5 (two-piece gap-affine: + I2, D2).
 WFG_HD constexpr inline ArenaLayout wfg_arena_layout(int scope, int ring_w, int leaf_max_score, int leaf_words,
-                                           int run_cap, int leaf_run_cap, int stack_cap) {
+                                           int run_cap, int leaf_run_cap, int stack_cap, int ncomp = 3) {
   ArenaLayout L{};
   int64_t off = 0;
-  L.ring_off = off; L.ring_bytes = wfg_align256((int64_t)2 * scope * 3 * ring_w * 4); off += L.ring_bytes;
-  L.ldesc_off = off; L.ldesc_bytes = wfg_align256((int64_t)(leaf_max_score + 1) * 3 * 16); off += L.ldesc_bytes;
+  L.ring_off = off; L.ring_bytes = wfg_align256((int64_t)2 * scope * ncomp * ring_w * 4); off += L.ring_bytes;
+  L.ldesc_off = off; L.ldesc_bytes = wfg_align256((int64_t)(leaf_max_score + 1) * ncomp * 16); off += L.ldesc_bytes;
   L.ldata_off = off; L.ldata_bytes = wfg_align256((int64_t)leaf_words * 4); off += L.ldata_bytes;
   L.runs_off = off; L.runs_bytes = wfg_align256((int64_t)run_cap * 4); off += L.runs_bytes;
   L.lruns_off = off; L.lruns_bytes = wfg_align256((int64_t)leaf_run_cap * 4); off += L.lruns_bytes;
   L.stack_off = off; L.stack_bytes = wfg_align256((int64_t)stack_cap * 8 * 4); off += L.stack_bytes;
+  L.rdesc2_off = off; L.rdesc2_bytes = ncomp == 5 ? wfg_align256((int64_t)2 * 32 * 2 * 8) : 0; off += L.rdesc2_bytes;
   L.total = off;
   return L;
 }

@@ -175,15 +175,38 @@ int wfg_set_predictions(wfg_context_t* c, const float* pred) {
 namespace {
 
 // Internal penalties (WFA2-lib wavefront_penalties_set_affine, wavefront_penalties.c:95-130).
-struct IntPen { int x, o, e, scope, nphys; };
+// nc: stored components (3, or 5 for two gap pieces); emin: the cheapest gap base (bounds how
+// fast a wavefront widens with the score).
+struct IntPen {
+  int x, o, e, scope, nphys;
+  int o2 = 0, e2 = 0, nc = 3, emin = 1;
+};
 IntPen internal_penalties(const wfg_config_t* cfg) {
   IntPen p;
+  if (cfg->metric == WFG_METRIC_GAP_AFFINE_2P) {
+    // wavefront_penalties_set_affine2p (wavefront_penalties.c:132-173);
+    // wavefront_components_dimensions_affine2p: scope max(x, o1+e1, o2+e2) + 1
+    if (cfg->match < 0) {
+      p.x = 2 * cfg->mismatch - 2 * cfg->match;
+      p.o = 2 * cfg->gap_opening; p.e = 2 * cfg->gap_extension - cfg->match;
+      p.o2 = 2 * cfg->gap_opening2; p.e2 = 2 * cfg->gap_extension2 - cfg->match;
+    } else {
+      p.x = cfg->mismatch; p.o = cfg->gap_opening; p.e = cfg->gap_extension;
+      p.o2 = cfg->gap_opening2; p.e2 = cfg->gap_extension2;
+    }
+    p.scope = std::max(std::max(p.o + p.e, p.o2 + p.e2), p.x) + 1;
+    p.nphys = wfg_ring_buffers_2p(p.x, p.o, p.e, p.o2, p.e2);
+    p.nc = 5;
+    p.emin = std::max(std::min(p.e, p.e2), 1);
+    return p;
+  }
   if (cfg->metric == WFG_METRIC_EDIT || cfg->metric == WFG_METRIC_INDEL) {
     // wavefront_penalties_set_edit / _indel: one component, a wavefront at every score,
     // max_score_scope 2 (wavefront_components.c:45-60). x bounds the score guard only
     // (an indel-distance mismatch is two indels).
     p.x = (cfg->metric == WFG_METRIC_EDIT) ? 1 : 2; p.o = 1; p.e = 1;
     p.scope = 2; p.nphys = 2;
+    p.emin = 1;
     return p;
   }
   if (cfg->metric == WFG_METRIC_GAP_LINEAR) {
@@ -194,6 +217,7 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
     p.e = 0;
     p.scope = std::max(p.x, p.o) + 1;
     p.nphys = wfg_ring_buffers(p.x, p.o, 0);
+    p.emin = 1;
     return p;
   }
   if (cfg->match < 0) {
@@ -205,6 +229,7 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
   }
   p.scope = std::max(p.o + p.e, p.x) + 1;
   p.nphys = wfg_ring_buffers(p.x, p.o, p.e);
+  p.emin = std::max(p.e, 1);
   return p;
 }
 
@@ -237,10 +262,10 @@ void size_launch(const wfg_context* c, const IntPen& p, int pass, int ring_w_hin
   s.leaf_run_cap = maxsum + 2;
   s.stack_cap = 64;
   // Leaf store bound: every non-null step of a leaf of score <= leaf_max_score allocates at
-  // most 3 * min(window + 8, 2*s/e + 8) offsets.
+  // most nc * min(window + 8, 2*s/emin + 8) offsets.
   int64_t leaf_full = 0;
   for (int sc = 0; sc <= s.leaf_max_score; ++sc)
-    leaf_full += 3LL * std::min<int64_t>(maxsum + 8, 2LL * sc / std::max(p.e, 1) + 8);
+    leaf_full += (int64_t)p.nc * std::min<int64_t>(maxsum + 8, 2LL * sc / p.emin + 8);
   leaf_full = std::min<int64_t>(leaf_full, (int64_t)1 << 28);
   if (pass == 0) {
     const uint32_t plain_cap = std::min<uint32_t>(ring_full, kPlainRingCap);
@@ -259,17 +284,17 @@ void size_launch(const wfg_context* c, const IntPen& p, int pass, int ring_w_hin
     // Both rings of the group in dynamic shared memory: the widest power of two that keeps
     // them within kSmemRingBytes; penalties with many live buffers fall back to HBM rings.
     int w = kSmemRingW;
-    while (w >= 64 && (int64_t)2 * p.nphys * 3 * w * 4 > kSmemRingBytes) w >>= 1;
+    while (w >= 64 && (int64_t)2 * p.nphys * p.nc * w * 4 > kSmemRingBytes) w >>= 1;
     if (w < 64) s.smem = 0;
     else s.ring_w = std::min(s.ring_w, w);
   }
   s.L = wfg_arena_layout(s.smem ? 0 : p.nphys, s.ring_w, s.leaf_max_score, s.leaf_words, s.run_cap, s.leaf_run_cap,
-                         s.stack_cap);
+                         s.stack_cap, p.nc);
 }
 
 // Groups that fit the device at once for a shape (persistent grid).
 int64_t max_groups(const wfg_context* c, const IntPen& p, const Launch& l) {
-  const size_t dyn = l.smem ? (size_t)2 * p.nphys * 3 * (size_t)l.ring_w * sizeof(int32_t) : 0;
+  const size_t dyn = l.smem ? (size_t)2 * p.nphys * p.nc * (size_t)l.ring_w * sizeof(int32_t) : 0;
   int bps = 0;
   if (biwfa_occupancy_shape(l.gw, l.smem, dyn, &bps) != cudaSuccess || bps < 1) {
     (void)cudaGetLastError();
@@ -285,7 +310,7 @@ extern "C" {
 int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   if (!c || !cfg) return WF_STATUS_UNSUPPORTED;
   if (cfg->metric != WFG_METRIC_GAP_AFFINE && cfg->metric != WFG_METRIC_EDIT && cfg->metric != WFG_METRIC_INDEL &&
-      cfg->metric != WFG_METRIC_GAP_LINEAR) {
+      cfg->metric != WFG_METRIC_GAP_LINEAR && cfg->metric != WFG_METRIC_GAP_AFFINE_2P) {
     c->err = "unknown distance metric";
     return WF_STATUS_UNSUPPORTED;
   }
@@ -298,12 +323,18 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     c->err = "penalties must satisfy match <= 0, mismatch > 0, gap_opening >= 0, gap_extension > 0";
     return WF_STATUS_UNSUPPORTED;
   }
+  if (cfg->metric == WFG_METRIC_GAP_AFFINE_2P &&
+      (cfg->match > 0 || cfg->mismatch <= 0 || cfg->gap_opening < 0 || cfg->gap_extension <= 0 ||
+       cfg->gap_opening2 < 0 || cfg->gap_extension2 <= 0)) {
+    c->err = "two-piece penalties must satisfy match <= 0, mismatch > 0, o1 >= 0, e1 > 0, o2 >= 0, e2 > 0";
+    return WF_STATUS_UNSUPPORTED;
+  }
   const IntPen p = internal_penalties(cfg);
   if (p.scope > 32) {
     c->err = "max_score_scope above 32 is not supported";
     return WF_STATUS_UNSUPPORTED;
   }
-  if ((int64_t)(c->max_sum + 16) * (int64_t)std::max(p.x, p.o + p.e) >= ((int64_t)1 << 26)) {
+  if ((int64_t)(c->max_sum + 16) * (int64_t)std::max(p.x, std::max(p.o + p.e, p.o2 + p.e2)) >= ((int64_t)1 << 26)) {
     c->err = "pair too long for 27-bit scores";
     return WF_STATUS_UNSUPPORTED;
   }
@@ -362,14 +393,14 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     const double m = c->tune.ring_margin;
     if (n_wide > 0) {
       Launch l; l.gw = c->tune.wide_warps; l.order_off = 0; l.count = n_wide;
-      const int w_need = (int)(m * max_wide / std::max(p.e, 1)) + 64;
+      const int w_need = (int)(m * max_wide / p.emin) + 64;
       l.smem = (c->tune.wide_smem && next_pow2((uint64_t)w_need) <= (uint32_t)kSmemRingW) ? 1 : 0;
       l.ring_w = w_need;
       first.push_back(l);
     }
     if (n_narrow > 0) {
       Launch l; l.gw = 1; l.order_off = n_wide; l.count = n_narrow;
-      l.ring_w = (int)(m * max_narrow / std::max(p.e, 1)) + 64;
+      l.ring_w = (int)(m * max_narrow / p.emin) + 64;
       first.push_back(l);
     }
   } else {
@@ -426,8 +457,9 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   if (n > 0 && !order_on_device) std::copy(order.begin(), order.end(), c->h_order_pin.ptr);
   auto params = [&](const Launch& l, int ps) {
     KernelParams kp{};
-    kp.x = p.x; kp.o = p.o; kp.e = p.e; kp.scope = p.scope;
+    kp.x = p.x; kp.o = p.o; kp.e = p.e; kp.scope = p.scope; kp.o2 = p.o2; kp.e2 = p.e2;
     kp.match_o = cfg->match; kp.x_o = cfg->mismatch; kp.o_o = cfg->gap_opening; kp.e_o = cfg->gap_extension;
+    if (p.nc == 5) { kp.o2_o = cfg->gap_opening2; kp.e2_o = cfg->gap_extension2; }
     kp.metric = cfg->metric;
     kp.score_only = cfg->score_only;
     kp.max_steps = cfg->max_alignment_steps > 0 ? cfg->max_alignment_steps : INT_MAX;

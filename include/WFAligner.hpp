@@ -189,9 +189,7 @@ class WFAligner {
   bool heuristic_unsupported_ = false;  // a heuristic other than none was requested
 
   void refresh() {
-    unsupported_ = heuristic_unsupported_ ||
-                   attributes.distance_metric == gap_affine_2p ||
-                   attributes.memory_mode != wavefront_memory_ultralow;
+    unsupported_ = heuristic_unsupported_ || attributes.memory_mode != wavefront_memory_ultralow;
   }
   AlignmentStatus unsupported() {
     if (wfAligner) {
@@ -215,8 +213,8 @@ class WFAligner {
   WFAligner& operator=(const WFAligner&) = delete;
 };
 
-// The other distances keep WFA2-lib's class names; indel, edit and gap-linear run on the GPU,
-// two-piece affine aligners report StatusUnsupported.
+// The other distances keep WFA2-lib's class names; all of them (indel, edit, gap-linear,
+// gap-affine, two-piece gap-affine) run on the GPU.
 class WFAlignerIndel : public WFAligner {
  public:
   WFAlignerIndel(const AlignmentScope alignmentScope, const MemoryModel memoryModel = MemoryHigh)

@@ -212,11 +212,14 @@ int wavefront_batch_cigar(wavefront_aligner_t* const wf_aligner, const int pair,
  * as WFA2-lib aligners). */
 typedef struct wfg_context wfg_context_t;
 
-/* Distances of wfg_config_t.metric: WFA2-lib's gap_affine (default), edit, indel and gap_linear
- * (wavefront/wavefront_penalties.c:39-94). Edit and indel ignore the penalties; gap-linear
- * takes its indel penalty from gap_opening (match <= 0, mismatch > 0, indel > 0). */
+/* Distances of wfg_config_t.metric: WFA2-lib's gap_affine (default), edit, indel, gap_linear
+ * and gap_affine_2p (wavefront/wavefront_penalties.c:39-173). Edit and indel ignore the
+ * penalties; gap-linear takes its indel penalty from gap_opening (match <= 0, mismatch > 0,
+ * indel > 0); two-piece gap-affine reads (gap_opening, gap_extension) as the first piece and
+ * (gap_opening2, gap_extension2) as the second. */
 typedef enum {
-  WFG_METRIC_GAP_AFFINE = 0, WFG_METRIC_EDIT = 1, WFG_METRIC_INDEL = 2, WFG_METRIC_GAP_LINEAR = 3
+  WFG_METRIC_GAP_AFFINE = 0, WFG_METRIC_EDIT = 1, WFG_METRIC_INDEL = 2, WFG_METRIC_GAP_LINEAR = 3,
+  WFG_METRIC_GAP_AFFINE_2P = 4
 } wfg_metric_t;
 
 typedef struct {
@@ -224,6 +227,7 @@ typedef struct {
   int score_only;                                  /* 1: score only (compute_score scope) */
   int max_alignment_steps;                         /* <= 0: unlimited (WFA2 default INT_MAX) */
   int metric;                                      /* wfg_metric_t; scores of edit/indel are distances */
+  int gap_opening2, gap_extension2;                /* second gap piece (WFG_METRIC_GAP_AFFINE_2P) */
 } wfg_config_t;
 
 /* Scheduling policy of wfg_run. */

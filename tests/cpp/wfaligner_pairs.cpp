@@ -13,8 +13,7 @@ int main(int argc, char** argv) {
   using wfa::WFAligner;
   if (argc > 1 && std::string(argv[1]) == "--config-only") {
     wfa::WFAlignerGapAffine high(4, 6, 2, WFAligner::Alignment);  // default MemoryHigh
-    wfa::WFAlignerGapAffine2Pieces affine2p(4, 6, 2, 24, 1, WFAligner::Alignment, WFAligner::MemoryUltralow);
-    affine2p.setHeuristicNone();
+    wfa::WFAlignerGapAffine2Pieces affine2p(4, 6, 2, 24, 1, WFAligner::Alignment);  // default MemoryHigh
     wfa::WFAlignerGapAffine dflt(4, 6, 2, WFAligner::Alignment, WFAligner::MemoryUltralow);
     wfa::WFAlignerGapAffine ul(4, 6, 2, WFAligner::Alignment, WFAligner::MemoryUltralow);
     ul.setHeuristicNone();
@@ -29,7 +28,11 @@ int main(int argc, char** argv) {
     std::cout << "cigar_after_refusal\t[" << ul.getCIGAR(true) << "]\n";
     return 0;
   }
-  wfa::WFAlignerGapAffine aligner(4, 6, 2, WFAligner::Alignment, WFAligner::MemoryUltralow);
+  // --affine2p: the two-piece distance (0,4,6,2,24,1); otherwise gap-affine (0,4,6,2)
+  const bool two = argc > 1 && std::string(argv[1]) == "--affine2p";
+  wfa::WFAlignerGapAffine affine(4, 6, 2, WFAligner::Alignment, WFAligner::MemoryUltralow);
+  wfa::WFAlignerGapAffine2Pieces affine2p(4, 6, 2, 24, 1, WFAligner::Alignment, WFAligner::MemoryUltralow);
+  WFAligner& aligner = two ? static_cast<WFAligner&>(affine2p) : static_cast<WFAligner&>(affine);
   aligner.setHeuristicNone();  // WFA2-lib's default attributes carry the wf-adaptive heuristic
   std::vector<std::string> ps, ts;
   std::string line;

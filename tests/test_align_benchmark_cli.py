@@ -26,7 +26,8 @@ def test_cli_options():
     exe = _cli()
     assert subprocess.run([exe, "--help"], capture_output=True).returncode == 0
     for bad in (["-i", "x.seq", "--wfa-memory", "high"], ["-i", "x.seq", "--wfa-heuristic", "wfa-adaptive"],
-                ["-i", "x.seq", "-a", "gap-affine2p-wfa"], ["-i", "x.seq", "--wfa-span", "extension"],
+                ["-i", "x.seq", "-a", "gap-affine2p-dp"], ["-i", "x.seq", "--affine2p-penalties", "0,4,6,2"],
+                ["-i", "x.seq", "--wfa-span", "extension"],
                 ["-i", "x.seq", "--bogus"], ["-g", "0,4,6"]):
         r = subprocess.run([exe, *bad], capture_output=True, text=True)
         assert r.returncode == 1 and r.stderr, bad
@@ -35,7 +36,8 @@ def test_cli_options():
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["test.biwfa.affine.alg", "test.biwfa.score.affine.alg",
                                   "test.biwfa.affine.p1.alg", "test.biwfa.affine.p4.alg",
-                                  "test.biwfa.edit.alg", "test.biwfa.indel.alg", "test.biwfa.score.edit.alg"])
+                                  "test.biwfa.edit.alg", "test.biwfa.indel.alg", "test.biwfa.score.edit.alg",
+                                  "test.biwfa.affine2p.alg", "test.biwfa.score.affine2p.alg"])
 def test_cli_reproduces_wfa2_utest_outputs(tmp_path, name):
     exe = _cli()
     data = utest()
@@ -43,11 +45,13 @@ def test_cli_reproduces_wfa2_utest_outputs(tmp_path, name):
     seq = tmp_path / "in.seq"
     out = tmp_path / "out.alg"
     _write_seq(seq, data["pairs"])
-    algo = {0: "gap-affine-wfa", 1: "edit-wfa", 2: "indel-wfa"}[s.get("metric", 0)]
+    algo = {0: "gap-affine-wfa", 1: "edit-wfa", 2: "indel-wfa", 4: "gap-affine2p-wfa"}[s.get("metric", 0)]
     args = [exe, "-a", algo, "-i", str(seq), "-o", str(out), "--wfa-memory", "ultralow",
             "--wfa-heuristic", "none", "--batch-size", "97", "-q"]
     if algo == "gap-affine-wfa":
         args += ["-g", ",".join(map(str, s["penalties"]))]
+    if algo == "gap-affine2p-wfa":
+        args += ["--affine2p-penalties", ",".join(map(str, s["penalties"]))]
     if s["score_only"]:
         args.append("--wfa-score-only")
     subprocess.run(args, check=True)

@@ -42,8 +42,9 @@ def test_cpp_binding_reports_unsupported_configurations(tmp_path):
     out = subprocess.run([str(exe), "--config-only"], capture_output=True, text=True, check=True).stdout
     rows = dict(line.split("\t", 1) for line in out.strip().splitlines())
     unsupported = str(_capi.WF_STATUS_UNSUPPORTED)
-    # MemoryHigh (the binding's default), two-piece affine, WFA2-lib's default heuristic,
-    # an explicit heuristic and ends-free all refuse with a status instead of exiting
+    # MemoryHigh (the binding's default, for gap-affine and two-piece affine), WFA2-lib's
+    # default heuristic, an explicit heuristic and ends-free all refuse with a status instead
+    # of exiting
     for key in ("default_heuristic", "high", "affine2p", "heuristic", "endsfree"):
         assert rows[key] == unsupported, (key, rows[key])
     assert rows["no_device"] in ("0", str(_capi.WF_STATUS_DEVICE_ERROR))
@@ -52,19 +53,22 @@ def test_cpp_binding_reports_unsupported_configurations(tmp_path):
 
 
 @pytest.mark.gpu
-def test_cpp_binding_matches_oracle(tmp_path):
+@pytest.mark.parametrize("two_piece", [False, True])
+def test_cpp_binding_matches_oracle(tmp_path, two_piece):
     exe = _build(tmp_path)
     pairs = [(p, t) for p, t in utest()["pairs"][:120]]
     b = pkg.PairBatch.generate(1, 40, seed=8)
     pairs += [(b.pattern(i).decode(), b.text(i).decode()) for i in range(b.n)]
     pairs += [("", ""), ("ACGT", ""), ("", "ACGT")]
     stdin = "".join(f"{p}\t{t}\n" for p, t in pairs)
-    out = subprocess.run([str(exe)], input=stdin, capture_output=True, text=True, check=True).stdout.splitlines()
+    args = [str(exe)] + (["--affine2p"] if two_piece else [])
+    pen, metric = ((0, 4, 6, 2, 24, 1), binding.METRIC_AFFINE2P) if two_piece else ((0, 4, 6, 2), binding.METRIC_AFFINE)
+    out = subprocess.run(args, input=stdin, capture_output=True, text=True, check=True).stdout.splitlines()
     single = [line.split("\t") for line in out if not line.startswith("batch\t")]
     batch = [line.split("\t")[1:] for line in out if line.startswith("batch\t")]
     assert len(single) == len(pairs) and len(batch) == len(pairs)
     for i, (p, t) in enumerate(pairs):
-        st, score, ops, _ = binding.oracle_align(p.encode(), t.encode())
+        st, score, ops, _ = binding.oracle_align(p.encode(), t.encode(), pen, metric=metric)
         assert int(single[i][0]) == 0 and int(batch[i][0]) == 0, i
         if ops:
             assert int(single[i][1]) == score and int(batch[i][1]) == score, i

@@ -55,16 +55,20 @@ def test_gpu_matches_oracle_on_generated(batch_aligner, workload, n, seed):
     assert not bad, f"{len(bad)} pairs differ, first {bad[:5]}"
 
 
-LINEAR_METRICS = [(_capi.METRIC_EDIT, (0, 0, 0, 0)), (_capi.METRIC_INDEL, (0, 0, 0, 0)),
-                  (_capi.METRIC_GAP_LINEAR, (0, 4, 2, 0)), (_capi.METRIC_GAP_LINEAR, (-3, 2, 3, 0))]
-LINEAR_IDS = ["edit", "indel", "gap_linear_0_4_2", "gap_linear_m3_2_3"]
+OTHER_METRICS = [(_capi.METRIC_EDIT, (0, 0, 0, 0)), (_capi.METRIC_INDEL, (0, 0, 0, 0)),
+                 (_capi.METRIC_GAP_LINEAR, (0, 4, 2, 0)), (_capi.METRIC_GAP_LINEAR, (-3, 2, 3, 0)),
+                 (_capi.METRIC_GAP_AFFINE_2P, (0, 4, 6, 2, 24, 1)), (_capi.METRIC_GAP_AFFINE_2P, (-2, 3, 1, 2, 8, 1)),
+                 (_capi.METRIC_GAP_AFFINE_2P, (0, 4, 12, 1, 3, 4))]
+OTHER_IDS = ["edit", "indel", "gap_linear_0_4_2", "gap_linear_m3_2_3", "affine2p_0_4_6_2_24_1",
+             "affine2p_m2_3_1_2_8_1", "affine2p_0_4_12_1_3_4"]
 
 
-@pytest.mark.parametrize("metric,pen", LINEAR_METRICS, ids=LINEAR_IDS)
+@pytest.mark.parametrize("metric,pen", OTHER_METRICS, ids=OTHER_IDS)
 @pytest.mark.parametrize("workload,n,seed", [(1, 200, 31), (3, 120, 33), (5, 2000, 35)])
-def test_gpu_linear_distances_match_oracle(batch_aligner, metric, pen, workload, n, seed):
-    """Edit, indel and gap-linear BiWFA (WFA2-lib's edit-wfa / indel-wfa / gap-linear-wfa with
-    ultralow memory) against the oracle, full CIGARs and score-only."""
+def test_gpu_other_distances_match_oracle(batch_aligner, metric, pen, workload, n, seed):
+    """Edit, indel, gap-linear and two-piece gap-affine BiWFA (WFA2-lib's edit-wfa / indel-wfa /
+    gap-linear-wfa / gap-affine2p-wfa with ultralow memory) against the oracle, full CIGARs and
+    score-only."""
     b = pkg.PairBatch.generate(workload, n, seed)
     res = batch_aligner.align(b, penalties=pen, metric=metric)
     res_so = batch_aligner.align(b, penalties=pen, metric=metric, score_only=True)
@@ -78,8 +82,9 @@ def test_gpu_linear_distances_match_oracle(batch_aligner, metric, pen, workload,
     assert not bad, f"{len(bad)} pairs differ, first {bad[:5]}"
 
 
-@pytest.mark.parametrize("metric,pen", LINEAR_METRICS[:3], ids=LINEAR_IDS[:3])
-def test_gpu_linear_distances_through_retry_passes_and_shapes(batch_aligner, metric, pen):
+@pytest.mark.parametrize("metric,pen", [OTHER_METRICS[i] for i in (0, 1, 2, 4)],
+                         ids=[OTHER_IDS[i] for i in (0, 1, 2, 4)])
+def test_gpu_other_distances_through_retry_passes_and_shapes(batch_aligner, metric, pen):
     """Long pairs of very different lengths (edit's exact pruning), the retry passes of every
     shape and the multi-warp shapes give the single-warp results."""
     rng = np.random.default_rng(5)
