@@ -77,10 +77,11 @@ __device__ __forceinline__ WfRef absent_ref() {
 }
 
 // Internal penalties. metric: kMetricAffine, kMetricEdit, kMetricIndel, kMetricLinear (o =
-// indel, e = 0) or kMetricAffine2p (o, e the first gap piece, o2, e2 the second); go: the
+// indel, e = 0) or kMetricAffine2p (o, e the first gap piece; the second, o2/e2, is carried by
+// DirCfg so that the other distances' functions keep their register budget); go: the
 // gap-opening adjust of the overlap and its stop conditions (o for gap-affine, max(o, o2) for
 // two-piece gap-affine, 0 otherwise, wavefront/wavefront_bialign.c:396-410).
-struct Pen { int x, o, e, scope, metric, go, o2, e2; };
+struct Pen { int x, o, e, scope, metric, go; };
 constexpr int kMetricAffine = 0, kMetricEdit = 1, kMetricIndel = 2, kMetricLinear = 3, kMetricAffine2p = 4;
 
 // Oriented window over packed words (forward arrays for the forward aligner and the
@@ -193,6 +194,7 @@ struct DirCfg {
   int nphys;         // physical ring buffers (round-robin over non-null steps)
   int lmax;          // leaf descriptor capacity (scores)
   int nc;            // stored components: 3 (M, I1, D1) or 5 (+ I2, D2)
+  int o2, e2;        // second gap piece, internal (two-piece gap-affine)
   int2* rdesc;       // ring descriptors [scope*3] (shared memory)
   int2* rdesc2;      // I2/D2 ring descriptors [scope*2] (warp arena; nc == 5 only)
   int* rphys;        // physical buffer of each ring slot [scope] (shared memory)
@@ -258,25 +260,48 @@ __device__ __forceinline__ void set_desc(const DirCfg& c, int score, int ci, int
   }
 }
 
+// The five-component (two-piece gap-affine) form of dir_init's storage reset.
+__device__ __noinline__ void dir_init_5(const DirCfg& c, int cbi) {
+  if (!c.leaf) {
+    for (int i = 0; i < c.scope * 3; ++i) c.rdesc[i] = make_int2(kAbsent, INT_MIN);
+    for (int i = 0; i < c.scope * 2; ++i) c.rdesc2[i] = make_int2(kAbsent, INT_MIN);
+    for (int i = 0; i < c.scope; ++i) c.rphys[i] = 0;
+    set_desc<0>(c, 0, cbi, 0, 0, 0, 0);
+    // diagonal 0 of score 0 (physical buffer 0)
+    c.rdata[(size_t)(cbi < 3 ? cbi : c.nphys * 3 + (cbi - 3)) * c.W] = 0;
+  } else {
+    for (int ci = 0; ci < 5; ++ci) set_desc<1>(c, 0, ci, kAbsent, INT_MIN, 0, 0);
+    set_desc<1>(c, 0, cbi, 0, 0, 0, 0);
+    c.ldata[0] = 0;
+  }
+}
+
 // wavefront_aligner_init / init_wf (wavefront/wavefront_aligner.c:251-417). The caller
-// has passed a group barrier since the last read of d.
+// has passed a group barrier since the last read of d. TWO: two-piece gap-affine storage
+// (five components); the kernel is specialised on it so the three-component path carries
+// no trace of the other.
+template <bool TWO>
 __device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
   const DirCfg c = d.cfg;
   d.sv = sv; d.cb = cb; d.ce = ce;
   d.num_null = 0; d.status = ST_OK; d.status_score = 0; d.end_k = INT_MAX;
   const int cbi = comp_index(cb);
+  if (TWO) {
+    dir_init_5(c, cbi);
+    if (!c.leaf) d.next_phys = 1 % c.nphys;
+    else d.lused = 1;
+    return;
+  }
   if (!c.leaf) {
     for (int i = 0; i < c.scope * 3; ++i) c.rdesc[i] = make_int2(kAbsent, INT_MIN);
-    if (c.nc == 5) for (int i = 0; i < c.scope * 2; ++i) c.rdesc2[i] = make_int2(kAbsent, INT_MIN);
     for (int i = 0; i < c.scope; ++i) c.rphys[i] = 0;
-    set_desc<0>(c, 0, cbi, 0, 0, 0, 0);
-    // diagonal 0 of score 0 (physical buffer 0)
-    c.rdata[(size_t)(cbi < 3 ? cbi : c.nphys * 3 + (cbi - 3)) * c.W] = 0;
+    c.rdesc[cbi] = make_int2(0, 0);
+    c.rdata[(size_t)cbi * c.W] = 0;  // diagonal 0 of score 0 (physical buffer 0)
     d.next_phys = 1 % c.nphys;
   } else {
     d.lused = 1;
-    for (int ci = 0; ci < c.nc; ++ci) set_desc<1>(c, 0, ci, kAbsent, INT_MIN, 0, 0);
-    set_desc<1>(c, 0, cbi, 0, 0, 0, 0);
+    for (int ci = 0; ci < 3; ++ci) c.ldesc[ci] = make_int4(kAbsent, INT_MIN, 0, 0);
+    c.ldesc[cbi] = make_int4(0, 0, 0, 0);
     c.ldata[0] = 0;
   }
 }
@@ -438,9 +463,9 @@ __device__ __noinline__ int dir_step_2p(Dir& d, const Pen p, int s, const Grp<G>
   const WfRef mo1 = fetch<MODE>(c, s - p.o - p.e, 0);
   const WfRef ie1 = fetch<MODE>(c, s - p.e, 1);
   const WfRef de1 = fetch<MODE>(c, s - p.e, 2);
-  const WfRef mo2 = fetch<MODE>(c, s - p.o2 - p.e2, 0);
-  const WfRef ie2 = fetch<MODE>(c, s - p.e2, 3);
-  const WfRef de2 = fetch<MODE>(c, s - p.e2, 4);
+  const WfRef mo2 = fetch<MODE>(c, s - c.o2 - c.e2, 0);
+  const WfRef ie2 = fetch<MODE>(c, s - c.e2, 3);
+  const WfRef de2 = fetch<MODE>(c, s - c.e2, 4);
   const bool hx = mx.nonnull(), ho1 = mo1.nonnull(), hie1 = ie1.nonnull(), hde1 = de1.nonnull();
   const bool ho2 = mo2.nonnull(), hie2 = ie2.nonnull(), hde2 = de2.nonnull();
   if (!hx && !ho1 && !hie1 && !hde1 && !ho2 && !hie2 && !hde2) {
@@ -552,10 +577,10 @@ __device__ __noinline__ int dir_step_2p(Dir& d, const Pen p, int s, const Grp<G>
   return 0;
 }
 
-template <int G, int MODE>
+template <int G, int MODE, bool TWO>
 __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g, int* max_ak_out) {
+  if (TWO) return dir_step_2p<G, MODE>(d, p, s, g, max_ak_out);
   if (p.metric == kMetricEdit || p.metric == kMetricIndel) return dir_step_linear<G, MODE>(d, p, s, g, max_ak_out);
-  if (p.metric == kMetricAffine2p) return dir_step_2p<G, MODE>(d, p, s, g, max_ak_out);
   const DirCfg c = d.cfg;
   constexpr bool kLeaf = MODE == 1;  // the leaf store (else the modular rings)
   // gap-linear (wavefront_compute_linear, wavefront/wavefront_compute_linear.c:166-195): the
@@ -731,29 +756,50 @@ __device__ void bp_scan(bool is_m, bool fwd, int s0, int s1, const WfRef& w0, co
   }
 }
 
-// wavefront_bialign_overlap (wavefront/wavefront_bialign.c:314-392): for two-piece
-// gap-affine the I2/D2 pairs first (gap-open o2), then I1/D1 (o1), then M.
+// wavefront_bialign_overlap (wavefront/wavefront_bialign.c:314-392), two-piece gap-affine: the
+// I2/D2 pairs first (gap-open o2), then I1/D1 (o1), then M.
 template <int G>
+__device__ __noinline__ void overlap_2p(const Dir& d0, const Dir& d1, int s0, int s1, bool fwd, BP& bp, const Pen p,
+                                        const Grp<G> g) {
+  const DirCfg c0 = d0.cfg, c1 = d1.cfg;
+  const int plen = d0.sv.plen, tlen = d0.sv.tlen, o2 = c0.o2;
+  const WfRef m0 = ref_raw<0>(c0, s0, 0);
+  if (!m0.present()) return;
+  for (int i = 0; i < p.scope; ++i) {
+    const int si = s1 - i;
+    if (si < 0) break;
+    if (s0 + si - o2 >= bp.score) continue;
+    const WfRef dd20 = ref_raw<0>(c0, s0, 4), dd21 = ref_raw<0>(c1, si, 4);
+    if (dd20.present() && dd21.present()) bp_scan<G>(false, fwd, s0, si, dd20, dd21, plen, tlen, o2, CD2, bp, g);
+    const WfRef ii20 = ref_raw<0>(c0, s0, 3), ii21 = ref_raw<0>(c1, si, 3);
+    if (ii20.present() && ii21.present()) bp_scan<G>(false, fwd, s0, si, ii20, ii21, plen, tlen, o2, CI2, bp, g);
+    if (s0 + si - p.o >= bp.score) continue;
+    const WfRef dd0 = ref_raw<0>(c0, s0, 2), dd1 = ref_raw<0>(c1, si, 2);
+    if (dd0.present() && dd1.present()) bp_scan<G>(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, g);
+    const WfRef ii0 = ref_raw<0>(c0, s0, 1), ii1 = ref_raw<0>(c1, si, 1);
+    if (ii0.present() && ii1.present()) bp_scan<G>(false, fwd, s0, si, ii0, ii1, plen, tlen, p.o, CI, bp, g);
+    if (s0 + si >= bp.score) continue;
+    const WfRef mm1 = ref_raw<0>(c1, si, 0);
+    if (mm1.present()) bp_scan<G>(true, fwd, s0, si, m0, mm1, plen, tlen, p.o, CM, bp, g);
+  }
+}
+
+// wavefront_bialign_overlap (wavefront/wavefront_bialign.c:314-392): I/D pairs (gap-affine),
+// then M (every distance).
+template <int G, bool TWO>
 __device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s1, bool fwd, BP& bp, const Pen p,
                                      const Grp<G> g) {
+  if (TWO) { overlap_2p<G>(d0, d1, s0, s1, fwd, bp, p, g); return; }
   const DirCfg c0 = d0.cfg, c1 = d1.cfg;
   const int plen = d0.sv.plen, tlen = d0.sv.tlen;
   const WfRef m0 = ref_raw<0>(c0, s0, 0);
   if (!m0.present()) return;
   const WfRef dd0 = ref_raw<0>(c0, s0, 2);
   const WfRef ii0 = ref_raw<0>(c0, s0, 1);
-  const bool two = p.metric == kMetricAffine2p;
   for (int i = 0; i < p.scope; ++i) {
     const int si = s1 - i;
     if (si < 0) break;
-    if (two) {
-      if (s0 + si - p.o2 >= bp.score) continue;
-      const WfRef dd20 = ref_raw<0>(c0, s0, 4), dd21 = ref_raw<0>(c1, si, 4);
-      if (dd20.present() && dd21.present()) bp_scan<G>(false, fwd, s0, si, dd20, dd21, plen, tlen, p.o2, CD2, bp, g);
-      const WfRef ii20 = ref_raw<0>(c0, s0, 3), ii21 = ref_raw<0>(c1, si, 3);
-      if (ii20.present() && ii21.present()) bp_scan<G>(false, fwd, s0, si, ii20, ii21, plen, tlen, p.o2, CI2, bp, g);
-    }
-    if (s0 + si - (two ? p.o : p.go) >= bp.score) continue;
+    if (s0 + si - p.go >= bp.score) continue;
     const WfRef dd1 = ref_raw<0>(c1, si, 2);
     if (dd0.present() && dd1.present()) bp_scan<G>(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, g);
     const WfRef ii1 = ref_raw<0>(c1, si, 1);
@@ -788,12 +834,12 @@ __device__ __forceinline__ int score_guard(const Pen& p, int plen, int tlen) {
 }
 
 // wavefront_bialign_find_breakpoint
-template <int G>
+template <int G, bool TWO>
 __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, int pb, int pe, int tb, int te,
                                             int cb, int ce, const Pen p, int max_steps, BP& bp, const Grp<G> g) {
   g.sync();
-  dir_init(F, fwd_view(q, pb, pe, tb, te), cb, ce);
-  dir_init(R, rev_view(q, pb, pe, tb, te), ce, cb);
+  dir_init<TWO>(F, fwd_view(q, pb, pe, tb, te), cb, ce);
+  dir_init<TWO>(R, rev_view(q, pb, pe, tb, te), ce, cb);
   g.sync();
   const int plen = pe - pb, tlen = te - tb;
   const int max_antidiag = plen + tlen - 1;
@@ -806,14 +852,14 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
   for (;;) {
     if (fmax + rmax >= max_antidiag) break;
     ++sf;
-    const int qf = dir_step<G, 0>(F, p, sf, g, &ak);
+    const int qf = dir_step<G, 0, TWO>(F, p, sf, g, &ak);
     if (qf < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (fmax < ak) fmax = ak;
     last_fwd = true;
     if (qf) return F.status;
     if (fmax + rmax >= max_antidiag) break;
     ++sr;
-    const int qr = dir_step<G, 0>(R, p, sr, g, &ak);
+    const int qr = dir_step<G, 0, TWO>(R, p, sr, g, &ak);
     if (qr < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (rmax < ak) rmax = ak;
     last_fwd = false;
@@ -825,17 +871,17 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
     if (last_fwd) {
       const int min_sr = (sr > p.scope - 1) ? sr - (p.scope - 1) : 0;
       if (sf + min_sr - p.go >= bp.score) break;
-      overlap<G>(F, R, sf, sr, true, bp, p, g);
+      overlap<G, TWO>(F, R, sf, sr, true, bp, p, g);
       ++sr;
-      const int q = dir_step<G, 0>(R, p, sr, g, &ak);
+      const int q = dir_step<G, 0, TWO>(R, p, sr, g, &ak);
       if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
       if (q) return R.status;
     }
     const int min_sf = (sf > p.scope - 1) ? sf - (p.scope - 1) : 0;
     if (min_sf + sr - p.go >= bp.score) break;
-    overlap<G>(R, F, sr, sf, false, bp, p, g);
+    overlap<G, TWO>(R, F, sr, sf, false, bp, p, g);
     ++sf;
-    const int q = dir_step<G, 0>(F, p, sf, g, &ak);
+    const int q = dir_step<G, 0, TWO>(F, p, sf, g, &ak);
     if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (q) return F.status;
     if (sr + sf >= max_steps) return WFG_ST_MAX_STEPS;
@@ -875,29 +921,12 @@ __device__ __forceinline__ long long bt_src(const DirCfg& B, int score, int ci, 
   return (long long)kNull;
 }
 
-// Leaf: wavefront_bialign_base -> unialign -> backtrace. Appends the leaf's ops to out.
-template <int G>
-__device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe, int tb, int te, int cb, int ce,
-                                       const Pen p, int max_steps, RunOut& out, uint32_t* lruns, int lruns_cap,
-                                       const Grp<G> g, int* max_leaf_score) {
-  g.sync();
-  dir_init(B, fwd_view(q, pb, pe, tb, te), cb, ce);
-  g.sync();
-  const int guard = score_guard(p, pe - pb, te - tb);
-  int s = 0, ak = 0;
-  if (!dir_extend<G>(B, s, g, nullptr)) {
-    for (;;) {
-      ++s;
-      // wavefront_unialign_reached_limits checks the step count after compute, before extend
-      if (s >= max_steps) return WFG_ST_UNATTAINABLE;
-      if (s > guard) return WFG_ST_UNATTAINABLE;
-      const int q = dir_step<G, 1>(B, p, s, g, &ak);
-      if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
-      if (q) break;
-    }
-  }
-  if (*max_leaf_score < s) *max_leaf_score = s;
-  if (B.status != ST_END_REACHED) return WFG_ST_UNATTAINABLE;
+// wavefront_backtrace_affine (wavefront/wavefront_backtrace.c:320-529; TWO: the two-piece
+// distance's I2/D2 sources) or wavefront_backtrace_linear (:223-319) over the leaf store, from
+// (end_k, tlen) at score s in component ce; appends the leaf's ops to out.
+template <bool TWO>
+__device__ __forceinline__ int leaf_backtrace(const Dir& B, const Pen p, int s, int ce, RunOut& out, uint32_t* lruns,
+                                              int lruns_cap) {
   const DirCfg bc = B.cfg;
   // Backtrace from (end_k, tlen) in component ce; runs are produced end -> begin. Every
   // thread of the group walks the same path (uniform loads, identical writes).
@@ -909,8 +938,8 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
     if (rlen > 0) { if (nrev < lruns_cap) lruns[nrev] = ((uint32_t)rlen << 4) | (uint32_t)rop; else rover = true; ++nrev; }
     rop = op; rlen = len;
   };
-  const bool lin = p.metric != kMetricAffine && p.metric != kMetricAffine2p;
-  const bool two = p.metric == kMetricAffine2p;
+  const bool lin = !TWO && p.metric != kMetricAffine;
+  constexpr bool two = TWO;
   int matrix = ce, score = s, k = B.end_k;
   int32_t off = tlen;
   int h = off, v = off - k;
@@ -925,7 +954,7 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
     // (wavefront/wavefront_backtrace.c:223-319): M sources only, gap-open = o, no mismatch
     // source for indel
     const int mm = score - p.x, go = score - p.o - (lin ? 0 : p.e), ge = score - p.e;
-    const int go2 = score - p.o2 - p.e2, ge2 = score - p.e2;  // second gap piece (two-piece only)
+    const int go2 = score - bc.o2 - bc.e2, ge2 = score - bc.e2;  // second gap piece (two-piece only)
     long long max_all;
     if (matrix == CM) {
       const long long mis = (p.metric == kMetricIndel) ? (long long)kNull : bt_src(bc, mm, 0, k, 1, BT_M);
@@ -951,7 +980,7 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
       const long long io = bt_src(bc, go, 0, k - 1, 1, BT_I_OPEN);
       const long long ix = bt_src(bc, ge, 1, k - 1, 1, BT_I_EXT);
       max_all = io >= ix ? io : ix;
-    } else if (matrix == CD) {
+    } else if (!TWO || matrix == CD) {
       const long long dop = bt_src(bc, go, 0, k + 1, 0, BT_D_OPEN);
       const long long dx = bt_src(bc, ge, 2, k + 1, 0, BT_D_EXT);
       max_all = dop >= dx ? dop : dx;
@@ -977,7 +1006,7 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
     else if (type == BT_I_OPEN) { score = go; matrix = CM; push(WFG_OP_INS, 1); --k; --off; }
     else if (type == BT_I_EXT) { score = ge; matrix = CI; push(WFG_OP_INS, 1); --k; --off; }
     else if (type == BT_D_OPEN) { score = go; matrix = CM; push(WFG_OP_DEL, 1); ++k; }
-    else if (type == BT_D_EXT) { score = ge; matrix = CD; push(WFG_OP_DEL, 1); ++k; }
+    else if (!TWO || type == BT_D_EXT) { score = ge; matrix = CD; push(WFG_OP_DEL, 1); ++k; }
     else if (type == BT_I2_OPEN) { score = go2; matrix = CM; push(WFG_OP_INS, 1); --k; --off; }
     else if (type == BT_I2_EXT) { score = ge2; matrix = CI2; push(WFG_OP_INS, 1); --k; --off; }
     else if (type == BT_D2_OPEN) { score = go2; matrix = CM; push(WFG_OP_DEL, 1); ++k; }
@@ -1002,6 +1031,38 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
     out.emit((int)(r & 15u), (int)(r >> 4));
   }
   return ST_OK;
+}
+
+__device__ __noinline__ int leaf_backtrace_2p(const Dir& B, const Pen p, int s, int ce, RunOut& out, uint32_t* lruns,
+                                             int lruns_cap) {
+  return leaf_backtrace<true>(B, p, s, ce, out, lruns, lruns_cap);
+}
+
+// Leaf: wavefront_bialign_base -> unialign -> backtrace. Appends the leaf's ops to out.
+template <int G, bool TWO>
+__device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe, int tb, int te, int cb, int ce,
+                                       const Pen p, int max_steps, RunOut& out, uint32_t* lruns, int lruns_cap,
+                                       const Grp<G> g, int* max_leaf_score) {
+  g.sync();
+  dir_init<TWO>(B, fwd_view(q, pb, pe, tb, te), cb, ce);
+  g.sync();
+  const int guard = score_guard(p, pe - pb, te - tb);
+  int s = 0, ak = 0;
+  if (!dir_extend<G>(B, s, g, nullptr)) {
+    for (;;) {
+      ++s;
+      // wavefront_unialign_reached_limits checks the step count after compute, before extend
+      if (s >= max_steps) return WFG_ST_UNATTAINABLE;
+      if (s > guard) return WFG_ST_UNATTAINABLE;
+      const int q = dir_step<G, 1, TWO>(B, p, s, g, &ak);
+      if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
+      if (q) break;
+    }
+  }
+  if (*max_leaf_score < s) *max_leaf_score = s;
+  if (B.status != ST_END_REACHED) return WFG_ST_UNATTAINABLE;
+  if (TWO) return leaf_backtrace_2p(B, p, s, ce, out, lruns, lruns_cap);
+  return leaf_backtrace<false>(B, p, s, ce, out, lruns, lruns_cap);
 }
 
 // cigar_score_gap_affine (alignment/cigar.c:277-303), cigar_score_gap_affine2p (:304-342: per
@@ -1043,7 +1104,9 @@ struct GroupSmem {
 
 // G warps per pair, GROUPS groups per block. RING_SMEM: the two rings of each group live
 // in dynamic shared memory (sized by the host for ring_w); otherwise in the warp arena.
-template <int G, int GROUPS, bool RING_SMEM, int MINB>
+// TWO: the two-piece gap-affine distance (five wavefront components); the other distances
+// run in the TWO = false instantiation.
+template <int G, int GROUPS, bool RING_SMEM, int MINB, bool TWO>
 __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel(KernelParams P) {
   __shared__ GroupSmem s_grp[GROUPS];
   extern __shared__ __align__(16) int32_t s_ring_dyn[];
@@ -1055,7 +1118,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
   g.red = S.red;
   const long long ggroup = (long long)blockIdx.x * GROUPS + gib;
   const int nphys = P.ring_nphys > 0 ? P.ring_nphys : P.scope;
-  const int nc = P.metric == kMetricAffine2p ? 5 : 3;
+  const int nc = TWO ? 5 : 3;
   const ArenaLayout L = wfg_arena_layout(RING_SMEM ? 0 : nphys, P.ring_w, P.leaf_max_score, P.leaf_words,
                                          P.run_cap, P.leaf_run_cap, P.stack_cap, nc);
   uint8_t* arena = P.arena + ggroup * P.arena_bytes;
@@ -1074,19 +1137,20 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
   DirCfg fc{};
   int2* rdesc2 = (int2*)(arena + L.rdesc2_off);  // I2/D2 ring descriptors of both directions
   fc.leaf = 0; fc.scope = P.scope; fc.magic = magic; fc.W = P.ring_w; fc.nphys = nphys; fc.lmax = 0; fc.nc = nc;
+  fc.o2 = P.o2; fc.e2 = P.e2;
   fc.rdesc = S.rdesc[0]; fc.rdesc2 = rdesc2; fc.rphys = S.rphys[0]; fc.rdata = ring;
   DirCfg rc = fc;
   rc.rdesc = S.rdesc[1]; rc.rdesc2 = rdesc2 + kMaxScope * 2; rc.rphys = S.rphys[1]; rc.rdata = ring + ring_dir;
   DirCfg bcfg{};
   bcfg.leaf = 1; bcfg.scope = P.scope; bcfg.magic = magic; bcfg.W = 0; bcfg.nphys = 1; bcfg.lmax = P.leaf_max_score;
-  bcfg.nc = nc;
+  bcfg.nc = nc; bcfg.o2 = P.o2; bcfg.e2 = P.e2;
   bcfg.ldesc = ldesc; bcfg.ldata = ldata;
   F.cfg = fc; R.cfg = rc; B.cfg = bcfg;
   F.lcap = R.lcap = 0; F.lused = R.lused = 0;
   B.lcap = P.leaf_words; B.lused = 0;
   g.sync();
   const int go = P.metric == kMetricAffine ? P.o : P.metric == kMetricAffine2p ? max(P.o, P.o2) : 0;
-  const Pen pen = {P.x, P.o, P.e, P.scope, P.metric, go, P.o2, P.e2};
+  const Pen pen = {P.x, P.o, P.e, P.scope, P.metric, go};
 
   const unsigned long long num_pairs =
       P.num_pairs_ptr ? *P.num_pairs_ptr : (unsigned long long)P.num_pairs;
@@ -1114,7 +1178,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
     if (P.score_only) {
       // wavefront_bialign_compute_score (wavefront/wavefront_bialign.c:662-699)
       BP bp;
-      const int st = find_breakpoint<G>(F, R, q, 0, q.plen, 0, q.tlen, CM, CM, pen, P.max_steps, bp, g);
+      const int st = find_breakpoint<G, TWO>(F, R, q, 0, q.plen, 0, q.tlen, CM, CM, pen, P.max_steps, bp, g);
       if (st == ST_OK || st == ST_END_REACHED) {
         const int wf = (st == ST_END_REACHED) ? (F.status == ST_END_REACHED ? F.status_score : R.status_score) : bp.score;
         score = classic_score(P.metric, P.match_o, q.plen, q.tlen, wf);
@@ -1144,18 +1208,18 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
         if (tl == 0) { out.emit(WFG_OP_DEL, pl); continue; }
         if (pl == 0) { out.emit(WFG_OP_INS, tl); continue; }
         if (rem <= kFallbackMinScore) {
-          const int st = leaf_align<G>(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns, P.leaf_run_cap, g,
+          const int st = leaf_align<G, TWO>(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns, P.leaf_run_cap, g,
                                        &max_leaf);
           if (st != ST_OK) status = st;
           continue;
         }
         BP bp;
-        const int st = find_breakpoint<G>(F, R, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, bp, g);
+        const int st = find_breakpoint<G, TWO>(F, R, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, bp, g);
         if (st != ST_OK) {
           if (st == ST_END_REACHED) {
             const int reached = (F.status == ST_END_REACHED) ? F.status_score : R.status_score;
             if (reached <= kRecoveryMinScore) {
-              const int st2 = leaf_align<G>(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns,
+              const int st2 = leaf_align<G, TWO>(B, q, pb, pe, tb, te, cb, ce, pen, P.max_steps, out, lruns,
                                             P.leaf_run_cap, g, &max_leaf);
               if (st2 != ST_OK) status = st2;
             } else {
@@ -1266,20 +1330,57 @@ __global__ void pack_pairs_kernel(int n, const uint8_t* __restrict__ ascii, Pair
 // ------------------------------------------------------------------ host launchers
 namespace {
 
-// Execution shapes: (warps per pair, groups per block, rings in shared memory).
-template <int G, int GROUPS, bool RS, int MINB>
+// Execution shapes: (warps per pair, groups per block, rings in shared memory), each in a
+// three-component and a five-component (two-piece gap-affine) instantiation.
+template <int G, int GROUPS, bool RS, int MINB, bool TWO>
 cudaError_t launch_shape(const KernelParams& p, int grid, cudaStream_t stream) {
-  const size_t nc = p.metric == kMetricAffine2p ? 5 : 3;
-  const size_t dyn = RS ? (size_t)GROUPS * 2 * (size_t)(p.ring_nphys > 0 ? p.ring_nphys : p.scope) * nc *
+  const size_t dyn = RS ? (size_t)GROUPS * 2 * (size_t)(p.ring_nphys > 0 ? p.ring_nphys : p.scope) * (TWO ? 5 : 3) *
                               (size_t)p.ring_w * sizeof(int32_t)
                         : 0;
   if (dyn > 0) {
-    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB>,
+    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
   }
-  biwfa_persistent_kernel<G, GROUPS, RS, MINB><<<grid, G * GROUPS * 32, dyn, stream>>>(p);
+  biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO><<<grid, G * GROUPS * 32, dyn, stream>>>(p);
   return cudaGetLastError();
+}
+
+template <int G, int GROUPS, bool RS, int MINB, bool TWO>
+cudaError_t occupancy_of(size_t dyn, int* blocks_per_sm) {
+  if (dyn > 0) {
+    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO>,
+                                                       G * GROUPS * 32, dyn);
+}
+
+template <bool TWO>
+cudaError_t occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm) {
+  if (gw <= 1) return occupancy_of<1, 4, false, kMinBlocksPerSM, TWO>(0, blocks_per_sm);
+  if (gw == 8) {
+    if (ring_in_smem) return occupancy_of<8, 1, true, 1, TWO>(dyn, blocks_per_sm);
+    return occupancy_of<8, 1, false, 2, TWO>(0, blocks_per_sm);
+  }
+  if (ring_in_smem) return occupancy_of<4, 1, true, 1, TWO>(dyn, blocks_per_sm);
+  return occupancy_of<4, 1, false, 3, TWO>(0, blocks_per_sm);
+}
+
+template <bool TWO>
+cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) {
+  const int gw = p.group_warps > 0 ? p.group_warps : 1;
+  if (gw == 1) return launch_shape<1, 4, false, kMinBlocksPerSM, TWO>(p, grid, stream);
+  if (gw == 8) {
+    if (p.ring_in_smem) return launch_shape<8, 1, true, 1, TWO>(p, grid, stream);
+    return launch_shape<8, 1, false, 2, TWO>(p, grid, stream);
+  }
+  if (gw == 4) {
+    if (p.ring_in_smem) return launch_shape<4, 1, true, 1, TWO>(p, grid, stream);
+    return launch_shape<4, 1, false, 3, TWO>(p, grid, stream);
+  }
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -1287,33 +1388,14 @@ cudaError_t launch_shape(const KernelParams& p, int grid, cudaStream_t stream) {
 int biwfa_warps_per_block() { return 4; }
 
 cudaError_t biwfa_occupancy(int* blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<1, 4, false, kMinBlocksPerSM>,
-                                                       4 * 32, 0);
+  return occupancy_of<1, 4, false, kMinBlocksPerSM, false>(0, blocks_per_sm);
 }
 
-// Resident blocks per SM of a shape (dyn: its dynamic shared memory in bytes).
-cudaError_t biwfa_occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm) {
-  if (gw <= 1) return biwfa_occupancy(blocks_per_sm);
-  if (gw == 8) {
-    if (ring_in_smem) {
-      const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<8, 1, true, 1>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-      if (e != cudaSuccess) return e;
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<8, 1, true, 1>,
-                                                           8 * 32, dyn);
-    }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<8, 1, false, 2>,
-                                                         8 * 32, 0);
-  }
-  if (ring_in_smem) {
-    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<4, 1, true, 1>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<4, 1, true, 1>,
-                                                         4 * 32, dyn);
-  }
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<4, 1, false, 3>,
-                                                       4 * 32, 0);
+// Resident blocks per SM of a shape (dyn: its dynamic shared memory in bytes; two: the
+// two-piece gap-affine instantiation).
+cudaError_t biwfa_occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm, int two) {
+  return two ? occupancy_shape<true>(gw, ring_in_smem, dyn, blocks_per_sm)
+             : occupancy_shape<false>(gw, ring_in_smem, dyn, blocks_per_sm);
 }
 
 // Groups (pairs in flight) per block of a shape.
@@ -1323,17 +1405,7 @@ int biwfa_groups_per_block(int group_warps, int ring_in_smem) {
 }
 
 cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream) {
-  const int gw = p.group_warps > 0 ? p.group_warps : 1;
-  if (gw == 1) return launch_shape<1, 4, false, kMinBlocksPerSM>(p, grid, stream);
-  if (gw == 8) {
-    if (p.ring_in_smem) return launch_shape<8, 1, true, 1>(p, grid, stream);
-    return launch_shape<8, 1, false, 2>(p, grid, stream);
-  }
-  if (gw == 4) {
-    if (p.ring_in_smem) return launch_shape<4, 1, true, 1>(p, grid, stream);
-    return launch_shape<4, 1, false, 3>(p, grid, stream);
-  }
-  return cudaErrorInvalidValue;
+  return p.metric == kMetricAffine2p ? launch_kernel<true>(p, grid, stream) : launch_kernel<false>(p, grid, stream);
 }
 
 cudaError_t launch_pack(int n, const uint8_t* ascii, PairDesc* pairs, uint32_t* words, int num_sms,

@@ -296,7 +296,7 @@ void size_launch(const wfg_context* c, const IntPen& p, int pass, int ring_w_hin
 int64_t max_groups(const wfg_context* c, const IntPen& p, const Launch& l) {
   const size_t dyn = l.smem ? (size_t)2 * p.nphys * p.nc * (size_t)l.ring_w * sizeof(int32_t) : 0;
   int bps = 0;
-  if (biwfa_occupancy_shape(l.gw, l.smem, dyn, &bps) != cudaSuccess || bps < 1) {
+  if (biwfa_occupancy_shape(l.gw, l.smem, dyn, &bps, p.nc == 5) != cudaSuccess || bps < 1) {
     (void)cudaGetLastError();
     bps = 1;
   }
