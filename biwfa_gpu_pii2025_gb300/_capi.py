@@ -124,6 +124,9 @@ SIGNATURES = {
     "wavefront_aligner_set_max_alignment_steps": (None, [P(Aligner), C.c_int]),
     "cigar_sprint": (C.c_int, [C.c_char_p, P(Cigar), C.c_bool]),
     "cigar_score_gap_affine": (C.c_int, [P(Cigar), P(AffinePenalties)]),
+    "cigar_score_edit": (C.c_int, [P(Cigar)]),
+    "cigar_score_gap_linear": (C.c_int, [P(Cigar), P(LinearPenalties)]),
+    "cigar_score_gap_affine2p": (C.c_int, [P(Cigar), P(Affine2pPenalties)]),
     "cigar_get_CIGAR": (None, [P(Cigar), C.c_bool, P(_u32p), _ip]),
     "wavefront_align_batch": (C.c_int, [P(Aligner), C.c_int, P(C.c_char_p), _ip, P(C.c_char_p), _ip, _ip, _ip]),
     "wavefront_batch_cigar": (C.c_int, [P(Aligner), C.c_int, P(_u32p), _ip]),

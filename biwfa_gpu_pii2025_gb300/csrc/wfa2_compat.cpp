@@ -327,6 +327,46 @@ int cigar_score_gap_affine(const cigar_t* const cigar, const affine_penalties_t*
   return score;
 }
 
+// cigar_score_edit (alignment/cigar.c:244-259): every operation but a match counts one.
+int cigar_score_edit(const cigar_t* const cigar) {
+  int score = 0;
+  for (int i = cigar->begin_offset; i < cigar->end_offset; ++i) score += cigar->operations[i] != 'M';
+  return score;
+}
+
+// cigar_score_gap_linear (alignment/cigar.c:260-276)
+int cigar_score_gap_linear(const cigar_t* const cigar, const linear_penalties_t* const pen) {
+  int score = 0;
+  for (int i = cigar->begin_offset; i < cigar->end_offset; ++i) {
+    const char op = cigar->operations[i];
+    score -= op == 'M' ? pen->match : op == 'X' ? pen->mismatch : pen->indel;
+  }
+  return score;
+}
+
+// cigar_score_gap_affine2p (alignment/cigar.c:304-342): each maximal run of one operation at
+// once, a gap run at the cheaper of the two pieces. An empty CIGAR scores 0 here (WFA2-lib
+// aborts on it).
+int cigar_score_gap_affine2p(const cigar_t* const cigar, const affine2p_penalties_t* const pen) {
+  int score = 0;
+  int i = cigar->begin_offset;
+  while (i < cigar->end_offset) {
+    const char op = cigar->operations[i];
+    int j = i;
+    while (j < cigar->end_offset && cigar->operations[j] == op) ++j;
+    const int len = j - i;
+    if (op == 'M') score -= pen->match * len;
+    else if (op == 'X') score -= pen->mismatch * len;
+    else {
+      const int a = pen->gap_opening1 + pen->gap_extension1 * len;
+      const int b = pen->gap_opening2 + pen->gap_extension2 * len;
+      score -= a < b ? a : b;
+    }
+    i = j;
+  }
+  return score;
+}
+
 // cigar_get_CIGAR / cigar_compute_CIGAR (alignment/cigar.c:181-235). The buffer is owned
 // by the aligner that produced the cigar (valid until its next alignment).
 void cigar_get_CIGAR(cigar_t* const cigar, const bool show_mismatches, uint32_t** const cigar_buffer,

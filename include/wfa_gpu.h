@@ -188,6 +188,11 @@ void wavefront_aligner_set_max_alignment_steps(wavefront_aligner_t* const wf_ali
 int cigar_sprint(char* const buffer, const cigar_t* const cigar, const bool print_matches);
 /* alignment/cigar.h: cigar_score_gap_affine (cigar.c:277-303) */
 int cigar_score_gap_affine(const cigar_t* const cigar, const affine_penalties_t* const penalties);
+/* alignment/cigar.h: cigar_score_edit (cigar.c:244-259), cigar_score_gap_linear (:260-276),
+ * cigar_score_gap_affine2p (:304-342) */
+int cigar_score_edit(const cigar_t* const cigar);
+int cigar_score_gap_linear(const cigar_t* const cigar, const linear_penalties_t* const penalties);
+int cigar_score_gap_affine2p(const cigar_t* const cigar, const affine2p_penalties_t* const penalties);
 /* alignment/cigar.h: cigar_get_CIGAR (cigar.c:224-235); SAM BAM op codes, '='/'X' split
  * when show_mismatches. The buffer belongs to the cigar. */
 void cigar_get_CIGAR(cigar_t* const cigar, const bool show_mismatches,

@@ -87,3 +87,49 @@ def test_context_create_without_gpu_returns_null_or_works():
     if ctx:
         lib.wfg_context_destroy(ctx)
     assert lib.wfg_context_create(99) is None
+
+
+def _cigar_of(ops: str) -> "_capi.Cigar":
+    buf = C.create_string_buffer(ops.encode(), len(ops) + 1)
+    cg = _capi.Cigar()
+    cg.operations = C.cast(buf, C.POINTER(C.c_char))
+    cg.max_operations = len(ops) + 1
+    cg.begin_offset, cg.end_offset = 0, len(ops)
+    cg._buf = buf  # keep the buffer alive with the struct
+    return cg
+
+
+@pytest.mark.parametrize("metric,pen", [(0, (0, 4, 6, 2)), (0, (-3, 5, 3, 2)), (1, (0, 0, 0, 0)), (2, (0, 0, 0, 0)),
+                                        (3, (0, 4, 2, 0)), (4, (0, 4, 6, 2, 24, 1)), (4, (-2, 3, 1, 2, 8, 1))])
+def test_cigar_scorers_match_oracle_rescoring(metric, pen):
+    """cigar_score_gap_affine / _edit / _gap_linear / _gap_affine2p (host functions of the C
+    ABI) give the score align_benchmark prints for the oracle's CIGARs."""
+    from oracle import binding
+    lib = pkg.load_library()
+    rng = np.random.default_rng(metric * 10 + len(pen))
+    for _ in range(40):
+        n = int(rng.integers(1, 300))
+        p = bytes(rng.choice(list(b"ACGT"), n).astype(np.uint8))
+        t = bytearray(p)
+        for _ in range(int(rng.integers(0, 25))):
+            pos = int(rng.integers(0, max(len(t), 1)))
+            r = rng.random()
+            if r < 0.4 and t:
+                t[min(pos, len(t) - 1)] = int(rng.choice(list(b"ACGT")))
+            elif r < 0.7:
+                t[pos:pos] = bytes(rng.choice(list(b"ACGT"), int(rng.integers(1, 30))).astype(np.uint8))
+            else:
+                del t[pos:pos + int(rng.integers(1, 30))]
+        st, score, ops, _ = binding.oracle_align(p, bytes(t), pen, metric=metric)
+        if not ops:
+            continue
+        cg = _cigar_of(ops)
+        if metric == 0:
+            got = lib.cigar_score_gap_affine(C.byref(cg), C.byref(_capi.AffinePenalties(*pen)))
+        elif metric in (1, 2):
+            got = lib.cigar_score_edit(C.byref(cg))
+        elif metric == 3:
+            got = lib.cigar_score_gap_linear(C.byref(cg), C.byref(_capi.LinearPenalties(*pen[:3])))
+        else:
+            got = lib.cigar_score_gap_affine2p(C.byref(cg), C.byref(_capi.Affine2pPenalties(*pen)))
+        assert got == score, (metric, pen, ops)
