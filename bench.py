@@ -2,6 +2,7 @@
 """Benchmark: gap-affine BiWFA (score + CIGAR, bit-exact with WFA2-lib) on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload 1..5]
+    python bench.py --distances [--workload 1..5]   # one line per distance (WFA2-lib's metrics)
 
 A step aligns the whole synthetic batch once (pack + BiWFA on the device), inputs resident
 in HBM, L2 flushed before every step (512 MiB write). The default workload is the 1,000,000-
@@ -176,7 +177,8 @@ def profile_traffic():
     return None, ""
 
 
-def cpu_baseline(batch, sample_seconds: float = 12.0, threads: int | None = None):
+def cpu_baseline(batch, sample_seconds: float = 12.0, threads: int | None = None, metric: int = 0,
+                 penalties=PENALTIES):
     """The oracle (C restatement of WFA2-lib BiWFA) on all host cores over a bounded sample."""
     from oracle import binding
     threads = threads or os.cpu_count() or 1
@@ -188,7 +190,7 @@ def cpu_baseline(batch, sample_seconds: float = 12.0, threads: int | None = None
     while True:
         sub = batch.subset(order[:m2])
         secs, scores, status = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen,
-                                                         PENALTIES, threads=threads)
+                                                         penalties, threads=threads, metric=metric)
         if secs >= 0.5 * sample_seconds or m2 >= n:
             break
         m2 = int(min(n, m2 * max(2.0, min(8.0, sample_seconds / max(secs, 1e-3)))))
@@ -272,7 +274,7 @@ def time_path(al, sched, steps: int, warmup: int, dist, clocks=None):
         al.flush_l2(L2_FLUSH_BYTES)
         al.run(PENALTIES, sched=sched)
         al.synchronize()
-    step_ms, kernel_ms, launches = [], [], 0
+    step_ms, kernel_ms, launches, retried = [], [], 0, 0
     if clocks:
         clocks.start()
     dist.barrier()
@@ -287,8 +289,10 @@ def time_path(al, sched, steps: int, warmup: int, dist, clocks=None):
         st = al.stats()
         kernel_ms.append(st.kernel_ms)
         launches += st.launches
+        retried = max(retried, st.retried_pairs)
     dist.barrier()
     clk = clocks.stop() if clocks else None
+    time_path.retried = retried  # pairs that overflowed the first pass's scratch, per step
     return step_ms, kernel_ms, launches, clk
 
 
@@ -321,6 +325,7 @@ def run_ours(args):
                   if learned else "plain length-sorted batched launches")
     step_ms, kernel_ms, launches, clk = time_path(al, sched, args.steps, args.warmup, dist,
                                                   ClockSampler(local if world > 1 else 0))
+    retried = time_path.retried
     res = al.fetch()
     ok = int((res.status == 0).sum())
     same_as_plain = bool(np.array_equal(res.scores, plain_res.scores) and np.array_equal(res.status, plain_res.status)
@@ -375,6 +380,7 @@ def run_ours(args):
             "sorted_persistent_value": pairs_all / (t_sorted / 1e3), "sorted_persistent_ms_per_step": t_sorted,
             "learned_over_sorted_persistent": (t_sorted / t_step) if learned else None,
             "results_identical_to_plain": same_as_plain,
+            "retried_pairs_per_step": retried,
             "learned": learn_info,
             "e2e": {"value": dist.sum(float(n)) / (e2e_t / 1e3), "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t, "matches_device_run": e2e_ok,
@@ -399,6 +405,71 @@ def run_ours(args):
 
 
 SCHEDS = {"plain": 0, "learned": 1, "sorted": 3}
+
+# WFA2-lib's distances on the BiWFA path: (wfg metric, penalties as the library takes them)
+DISTANCES = {
+    "gap_affine (0,4,6,2)": (0, (0, 4, 6, 2)),
+    "gap_affine_2p (0,4,6,2,24,1)": (4, (0, 4, 6, 2, 24, 1)),
+    "gap_linear (0,4,2)": (3, (0, 4, 2, 0)),
+    "edit": (1, (0, 0, 0, 0)),
+    "indel": (2, (0, 0, 0, 0)),
+}
+
+
+def run_distances(args):
+    """One JSON line per distance: the sorted persistent and plain batched GPU paths on the
+    resident batch (L2 flushed before every step), a bit-exact check of a seeded sample against
+    the oracle, and the oracle on all host cores over a bounded sample of the same batch."""
+    import biwfa_gpu_pii2025_gb300 as pkg
+    from biwfa_gpu_pii2025_gb300 import _capi
+    from oracle import binding
+    wl = args.workload
+    name, n_full = WORKLOADS[wl]
+    n = args.pairs or n_full
+    al = pkg.BatchAligner(0)
+    batch = make_batch(wl, n, 0)
+    al.upload(batch)
+    cells = float((batch.plen.astype(np.float64) * batch.tlen).sum())
+    sample = np.random.default_rng(7).permutation(n)[:200]
+    for dname, (metric, pen) in DISTANCES.items():
+        times, retried = {}, {}
+        for sched_name in ("sorted", "plain"):
+            sched = SCHEDS[sched_name]
+            for _ in range(args.warmup):
+                al.flush_l2(L2_FLUSH_BYTES)
+                al.run(pen, sched=sched, metric=metric)
+                al.synchronize()
+            ms = []
+            for _ in range(args.steps):
+                al.flush_l2(L2_FLUSH_BYTES)
+                al.synchronize()
+                t0 = time.perf_counter()
+                al.run(pen, sched=sched, metric=metric)
+                al.synchronize()
+                ms.append(1e3 * (time.perf_counter() - t0))
+            times[sched_name] = statistics.mean(ms)
+            retried[sched_name] = al.stats().retried_pairs
+        res = al.fetch()
+        exact = True
+        for i in sample:
+            _, score, ops, _ = binding.oracle_align(batch.pattern(int(i)), batch.text(int(i)), pen, metric=metric)
+            if res.status[i] != 0 or pkg.runs_to_ops(res.runs_of(int(i))) != ops or res.scores[i] != (score if ops else 0):
+                exact = False
+                break
+        line = {"metric": f"pairs/s (exact score+CIGAR, BiWFA {dname}) on 1 GB300",
+                "distance": dname, "value": n / (times["sorted"] / 1e3), "unit": "pairs/s",
+                "ms_per_step": times["sorted"], "plain_value": n / (times["plain"] / 1e3),
+                "gcups": cells / (times["sorted"] / 1e3) / 1e9, "steps": args.steps, "warmup": args.warmup,
+                "pairs_ok": int((res.status == 0).sum()), "sample_bit_exact_vs_oracle": exact,
+                "retried_pairs_per_step": retried,
+                "config": {"workload": name, "num_pairs": n, "seed": SEED, "penalties": list(pen),
+                           "sched": "sorted persistent (value), plain batched (plain_value)",
+                           "l2": "flushed before every step (512 MiB write)"}}
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(batch, sample_seconds=8.0, metric=metric, penalties=pen)
+        print(json.dumps(line), flush=True)
+    al.close()
+    return 0
 
 
 def run_profile_case(args):
@@ -434,6 +505,8 @@ def main():
     ap.add_argument("--pairs", type=int, default=0, help="override the workload's pair count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time only the plain length-sorted path")
+    ap.add_argument("--distances", action="store_true",
+                    help="one line per distance (gap-affine, two-piece, gap-linear, edit, indel)")
     ap.add_argument("--profile-sched", choices=sorted(SCHEDS), default=None,
                     help="no timing: upload the batch, run the schedule warmup + steps times and exit "
                          "(the command the ncu captures in profiles/ run)")
@@ -444,6 +517,8 @@ def main():
         return run_reference(args)
     if args.profile_sched:
         return run_profile_case(args)
+    if args.distances:
+        return run_distances(args)
     return run_ours(args)
 
 

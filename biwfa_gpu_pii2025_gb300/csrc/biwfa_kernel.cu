@@ -220,20 +220,22 @@ __device__ __forceinline__ int slot_of(const DirCfg& c, int score) {
 }
 
 // MODE: 0 ring, 1 leaf store, -1 read from the configuration (callers that serve both).
+// An absent ring reference keeps the ring's base, kbase and mask (never dereferenced: its
+// range is empty), so that every ring reference of a step shares them.
 template <int MODE = -1>
 __device__ __forceinline__ WfRef ref_raw(const DirCfg& c, int score, int ci) {
-  if (score < 0) return absent_ref();
   WfRef r;
   const bool leaf = MODE < 0 ? (c.leaf != 0) : (MODE == 1);
   if (!leaf) {
+    r.kbase = 0; r.mask = (uint32_t)c.W - 1u;
+    if (score < 0) { r.lo = kAbsent; r.hi = INT_MIN; r.base = c.rdata; return r; }
     const int slot = slot_of(c, score);
     const int2 ds = ci < 3 ? c.rdesc[slot * 3 + ci] : c.rdesc2[slot * 2 + (ci - 3)];
     r.lo = ds.x; r.hi = ds.y;
     const int buf = ci < 3 ? c.rphys[slot] * 3 + ci : c.nphys * 3 + c.rphys[slot] * 2 + (ci - 3);
     r.base = c.rdata + (size_t)buf * (size_t)c.W;
-    r.kbase = 0; r.mask = (uint32_t)c.W - 1u;
   } else {
-    if (score > c.lmax) return absent_ref();
+    if (score < 0 || score > c.lmax) return absent_ref();
     const int4 ds = ci < 3 ? c.ldesc[score * 3 + ci] : c.ldesc[(c.lmax + 1) * 3 + score * 2 + (ci - 3)];
     r.lo = ds.x; r.hi = ds.y;
     r.base = c.ldata + ds.z;
@@ -245,8 +247,9 @@ __device__ __forceinline__ WfRef ref_raw(const DirCfg& c, int score, int ci) {
 // null (wavefront_compute_get_*wavefront).
 template <int MODE = -1>
 __device__ __forceinline__ WfRef fetch(const DirCfg& c, int score, int ci) {
-  const WfRef r = ref_raw<MODE>(c, score, ci);
-  return r.nonnull() ? r : absent_ref();
+  WfRef r = ref_raw<MODE>(c, score, ci);
+  if (!r.nonnull()) { r.lo = kAbsent; r.hi = INT_MIN; }
+  return r;
 }
 template <int MODE = -1>
 __device__ __forceinline__ void set_desc(const DirCfg& c, int score, int ci, int lo, int hi, int data_off, int kbase) {
@@ -1170,6 +1173,17 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
     q.pr = q.tf + pd.tw_len;
     q.tr = q.pr + pd.pw_len;
     q.plen = pd.plen; q.tlen = pd.tlen; q.bshift = (pd.bits == 2) ? 1 : 3;
+    {
+      // Rings sized to the pair: every wavefront of the pair (and of its sub-windows) lies on
+      // diagonals [-plen-1, tlen+1], so a ring of next_pow2(plen+tlen+8) <= ring_w diagonals
+      // never overflows; the two directions' rings are packed back to back at that width
+      // (a smaller footprint per warp for short pairs).
+      const uint32_t need = (uint32_t)(pd.plen + pd.tlen + 8);
+      const int wp = min(P.ring_w, max(64, (int)(1u << (32 - __clz((int)need - 1)))));
+      F.cfg.W = wp; R.cfg.W = wp;
+      F.cfg.rdata = ring;
+      R.cfg.rdata = ring + (size_t)nphys * nc * wp;
+    }
     int status = ST_OK;
     int score = 0;
     int nsteps = 0, max_leaf = -1, max_depth = 0;

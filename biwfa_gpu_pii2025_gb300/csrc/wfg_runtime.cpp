@@ -176,10 +176,11 @@ namespace {
 
 // Internal penalties (WFA2-lib wavefront_penalties_set_affine, wavefront_penalties.c:95-130).
 // nc: stored components (3, or 5 for two gap pieces); emin: the cheapest gap base (bounds how
-// fast a wavefront widens with the score).
+// fast a wavefront widens with the score); g: the spacing of the scores that can hold a
+// wavefront (the gcd of the step costs).
 struct IntPen {
   int x, o, e, scope, nphys;
-  int o2 = 0, e2 = 0, nc = 3, emin = 1;
+  int o2 = 0, e2 = 0, nc = 3, emin = 1, g = 1;
 };
 IntPen internal_penalties(const wfg_config_t* cfg) {
   IntPen p;
@@ -198,6 +199,7 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
     p.nphys = wfg_ring_buffers_2p(p.x, p.o, p.e, p.o2, p.e2);
     p.nc = 5;
     p.emin = std::max(std::min(p.e, p.e2), 1);
+    p.g = wfg_gcd(wfg_gcd(wfg_gcd(p.x, p.o + p.e), wfg_gcd(p.e, p.o2 + p.e2)), p.e2);
     return p;
   }
   if (cfg->metric == WFG_METRIC_EDIT || cfg->metric == WFG_METRIC_INDEL) {
@@ -206,7 +208,7 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
     // (an indel-distance mismatch is two indels).
     p.x = (cfg->metric == WFG_METRIC_EDIT) ? 1 : 2; p.o = 1; p.e = 1;
     p.scope = 2; p.nphys = 2;
-    p.emin = 1;
+    p.emin = 1; p.g = 1;
     return p;
   }
   if (cfg->metric == WFG_METRIC_GAP_LINEAR) {
@@ -217,7 +219,8 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
     p.e = 0;
     p.scope = std::max(p.x, p.o) + 1;
     p.nphys = wfg_ring_buffers(p.x, p.o, 0);
-    p.emin = 1;
+    p.emin = std::max(p.o, 1);  // one diagonal per indel on each side
+    p.g = wfg_gcd(p.x, p.o);
     return p;
   }
   if (cfg->match < 0) {
@@ -230,6 +233,7 @@ IntPen internal_penalties(const wfg_config_t* cfg) {
   p.scope = std::max(p.o + p.e, p.x) + 1;
   p.nphys = wfg_ring_buffers(p.x, p.o, p.e);
   p.emin = std::max(p.e, 1);
+  p.g = wfg_gcd(wfg_gcd(p.x, p.o + p.e), p.e);
   return p;
 }
 
@@ -261,20 +265,25 @@ void size_launch(const wfg_context* c, const IntPen& p, int pass, int ring_w_hin
   s.run_cap = maxsum + 2;
   s.leaf_run_cap = maxsum + 2;
   s.stack_cap = 64;
-  // Leaf store bound: every non-null step of a leaf of score <= leaf_max_score allocates at
-  // most nc * min(window + 8, 2*s/emin + 8) offsets.
-  int64_t leaf_full = 0;
-  for (int sc = 0; sc <= s.leaf_max_score; ++sc)
-    leaf_full += (int64_t)p.nc * std::min<int64_t>(maxsum + 8, 2LL * sc / p.emin + 8);
-  leaf_full = std::min<int64_t>(leaf_full, (int64_t)1 << 28);
+  // Leaf store bound: a leaf's wavefronts sit at scores that are multiples of g, and the step
+  // at score s allocates at most nc * min(window + 8, 2*s/emin + 8) offsets. Pass 0 holds a
+  // leaf that starts at the BiWFA fallback score (250) with room to spare, pass 1 four times
+  // that, pass 2 the full bound (recovery leaves up to score 500, whole short pairs).
+  auto leaf_words_upto = [&](int smax) {
+    int64_t w = 0;
+    for (int sc = 0; sc <= smax; sc += p.g) w += (int64_t)p.nc * std::min<int64_t>(maxsum + 8, 2LL * sc / p.emin + 8);
+    return w;
+  };
+  const int64_t leaf_full = std::min<int64_t>(leaf_words_upto(s.leaf_max_score), (int64_t)1 << 28);
+  const int64_t leaf_typical = leaf_words_upto(250) * 5 / 4;
   if (pass == 0) {
     const uint32_t plain_cap = std::min<uint32_t>(ring_full, kPlainRingCap);
     s.ring_w = ring_w_hint > 0 ? (int)std::min<uint32_t>(next_pow2((uint64_t)ring_w_hint), ring_full) : (int)plain_cap;
-    s.leaf_words = (int)std::min<int64_t>(leaf_full, 1 << 16);
+    s.leaf_words = (int)std::min<int64_t>(leaf_full, std::max<int64_t>(1 << 16, leaf_typical));
     if (c->limit_leaf_words > 0) s.leaf_words = std::max(c->limit_leaf_words, 16);
   } else if (pass == 1) {
     s.ring_w = (int)ring_full;
-    s.leaf_words = (int)std::min<int64_t>(leaf_full, 1 << 18);
+    s.leaf_words = (int)std::min<int64_t>(leaf_full, std::max<int64_t>(1 << 18, 4 * leaf_typical));
   } else {
     s.ring_w = (int)ring_full;
     s.leaf_words = (int)leaf_full;
@@ -417,7 +426,18 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   }
   if (first.empty()) { Launch l; l.count = 0; first.push_back(l); }
   // ---- shapes and arena (pass-0 launches run concurrently; retry passes reuse the arena)
-  const int64_t arena_budget = (int64_t)24 << 30;
+  // Arena budget: half of the device memory that is free or already held by the arena, within
+  // [4 GiB, 96 GiB] (one GB300 has 288 GB of HBM).
+  int64_t arena_budget = (int64_t)24 << 30;
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+      const int64_t avail = (int64_t)free_b + (int64_t)c->d_arena.cap;
+      arena_budget = std::min<int64_t>((int64_t)96 << 30, std::max<int64_t>((int64_t)4 << 30, avail / 2));
+    } else {
+      (void)cudaGetLastError();
+    }
+  }
   int64_t pass0_bytes = 0;
   for (Launch& l : first) {
     if (l.gw < 1) l.gw = 1;
