@@ -9,9 +9,9 @@
  * or the timed CPU baseline. The GPU product never calls it.
  *
  * Parity is pinned two ways (see tests/test_oracle.py):
- *   1. against WFA2-lib's own golden files for this path
- *      (tests/wfa.utest.check/test.biwfa.affine*.alg, test.biwfa.score.affine*.alg),
- *      carried as fixtures under tests/golden/;
+ *   1. against WFA2-lib's own golden files for these paths
+ *      (tests/wfa.utest.check/test.biwfa.affine*.alg, test.biwfa.score.affine*.alg,
+ *      test.biwfa{,.score}.{edit,indel,affine2p}.alg), carried as fixtures under tests/golden/;
  *   2. against the real WFA2-lib compiled from the reference sources
  *      (oracle/_ref/libwfa2_ref.so) on seeded random inputs.
  */
