@@ -270,6 +270,8 @@ def train_predictor(pkg, al, wl: int, n_train: int, rank: int):
 
 
 def time_path(al, sched, steps: int, warmup: int, dist, clocks=None):
+    """Times `steps` runs of one schedule; returns (step ms, kernel ms, launches, clocks,
+    largest number of pairs that took a retry pass in one step)."""
     for _ in range(warmup):
         al.flush_l2(L2_FLUSH_BYTES)
         al.run(PENALTIES, sched=sched)
@@ -292,8 +294,7 @@ def time_path(al, sched, steps: int, warmup: int, dist, clocks=None):
         retried = max(retried, st.retried_pairs)
     dist.barrier()
     clk = clocks.stop() if clocks else None
-    time_path.retried = retried  # pairs that overflowed the first pass's scratch, per step
-    return step_ms, kernel_ms, launches, clk
+    return step_ms, kernel_ms, launches, clk, retried
 
 
 def run_ours(args):
@@ -316,16 +317,15 @@ def run_ours(args):
     # ---- the plain length-sorted batched path (the comparison: one launch per resident set of
     # pairs, each waiting for its slowest pair), the length-sorted persistent path (ablation:
     # work stealing without the predictor), then the learned-binned persistent path (value)
-    plain_ms, plain_kernel_ms, _, _ = time_path(al, _capi.SCHED_PLAIN, args.steps, args.warmup, dist)
+    plain_ms, plain_kernel_ms, _, _, _ = time_path(al, _capi.SCHED_PLAIN, args.steps, args.warmup, dist)
     plain_res = al.fetch()
-    sorted_ms, _, _, _ = time_path(al, _capi.SCHED_SORTED, args.steps, args.warmup, dist)
+    sorted_ms, _, _, _, _ = time_path(al, _capi.SCHED_SORTED, args.steps, args.warmup, dist)
     sched = _capi.SCHED_LEARNED if learned else _capi.SCHED_PLAIN
     sched_name = ("learned-binned persistent (MLP score prediction orders and bins pairs, sizes scratch; "
                   "autotuned warps-per-pair and shared-memory rings)"
                   if learned else "plain length-sorted batched launches")
-    step_ms, kernel_ms, launches, clk = time_path(al, sched, args.steps, args.warmup, dist,
-                                                  ClockSampler(local if world > 1 else 0))
-    retried = time_path.retried
+    step_ms, kernel_ms, launches, clk, retried = time_path(al, sched, args.steps, args.warmup, dist,
+                                                           ClockSampler(local if world > 1 else 0))
     res = al.fetch()
     ok = int((res.status == 0).sum())
     same_as_plain = bool(np.array_equal(res.scores, plain_res.scores) and np.array_equal(res.status, plain_res.status)
