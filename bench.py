@@ -44,6 +44,14 @@ PENALTIES = (0, 4, 6, 2)
 SEED = 20251203
 TRAIN_SEED = 99991  # held-out seed of the predictor's training pairs
 L2_FLUSH_BYTES = 512 << 20
+# The port's single-thread speed relative to the real WFA2-lib on the same pairs (identical
+# scores), measured where both build (x86, oracle/calibrate_vs_wfa2.py): WFA2-lib itself is
+# absent on the GPU machine, so the reported CPU baseline is the port.
+PORT_CALIBRATION = {"port_speed_over_wfa2lib_median": {"mixture": 0.80, "1kbp_5pct": 1.08, "150bp_2pct": 1.15,
+                                                        "uneven": 0.79},
+                    "mixture_range": [0.71, 1.00],
+                    "measured_on": "x86_64 host, one thread each, one aligner reused across pairs, 5 alternating "
+                                   "runs per workload"}
 
 
 def dist_env():
@@ -197,7 +205,8 @@ def cpu_baseline(batch, sample_seconds: float = 12.0, threads: int | None = None
     cells = float((sub.plen.astype(np.float64) * sub.tlen).sum())
     return {"value": m2 / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
             "sample": f"{m2} pairs drawn uniformly (seed 99) from the same batch; {secs:.2f} s wall",
-            "gcups": cells / secs / 1e9}
+            "gcups": cells / secs / 1e9,
+            "calibration": PORT_CALIBRATION}
 
 
 def run_reference(args):

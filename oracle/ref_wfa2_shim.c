@@ -148,3 +148,32 @@ int ref_wfa_align_affine2p(const char* pattern, int plen, const char* text, int 
   wavefront_aligner_delete(wf);
   return status;
 }
+
+/* Timing helper: aligns n pairs (concatenated sequences, offsets and lengths as in the
+ * oracle's batch call) with ONE WFA2-lib aligner reused across pairs, as align_benchmark does
+ * per thread; full CIGAR, gap-affine penalties. Returns the wall-clock seconds of the loop and
+ * writes the printed scores (cigar_score_gap_affine of the CIGAR) to scores[]. */
+#include <time.h>
+double ref_biwfa_batch_time(int n, const char* seq, const long long* p_off, const int* plen, const long long* t_off,
+                            const int* tlen, int match, int mismatch, int gap_open, int gap_ext, int* scores) {
+  wavefront_aligner_attr_t attr = wavefront_aligner_attr_default;
+  attr.distance_metric = gap_affine;
+  attr.affine_penalties.match = match;
+  attr.affine_penalties.mismatch = mismatch;
+  attr.affine_penalties.gap_opening = gap_open;
+  attr.affine_penalties.gap_extension = gap_ext;
+  attr.memory_mode = wavefront_memory_ultralow;
+  attr.heuristic.strategy = wf_heuristic_none;
+  attr.alignment_scope = compute_alignment;
+  wavefront_aligner_t* const wf = wavefront_aligner_new(&attr);
+  affine_penalties_t pen = {match, mismatch, gap_open, gap_ext};
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  for (int i = 0; i < n; ++i) {
+    wavefront_align(wf, seq + p_off[i], plen[i], seq + t_off[i], tlen[i]);
+    scores[i] = (wf->cigar->begin_offset < wf->cigar->end_offset) ? cigar_score_gap_affine(wf->cigar, &pen) : -1;
+  }
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  wavefront_aligner_delete(wf);
+  return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
