@@ -29,7 +29,8 @@ namespace {
 constexpr int32_t kNull = INT32_MIN / 2;   // WAVEFRONT_OFFSET_NULL
 constexpr int kAbsent = INT32_MAX;         // lo of a wavefront that does not exist
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kMaxScope = 32;
+constexpr int kMaxScope = WFG_MAX_SCOPE;    // score scope cap of the three-component kernels
+constexpr int kMaxScope2p = WFG_MAX_SCOPE_2P;  // the same for two-piece gap-affine
 #ifndef WFG_G1_MIN_BLOCKS
 #define WFG_G1_MIN_BLOCKS 7
 #endif
@@ -1097,11 +1098,13 @@ __device__ __forceinline__ int classic_score(int metric, int match_o, int plen, 
 }  // namespace
 
 // Shared memory per group: three directions, ring descriptors and buffer map, reduction
-// scratch (dynamic shared memory holds the rings themselves when ring_in_smem).
+// scratch (dynamic shared memory holds the rings themselves when ring_in_smem). MS: the score
+// scope cap of the instantiation.
+template <int MS>
 struct GroupSmem {
   Dir dir[3];
-  int2 rdesc[2][kMaxScope * 3];
-  int rphys[2][kMaxScope];
+  int2 rdesc[2][MS * 3];
+  int rphys[2][MS];
   int red[8 * 8 + 8];
 };
 
@@ -1111,10 +1114,11 @@ struct GroupSmem {
 // run in the TWO = false instantiation.
 template <int G, int GROUPS, bool RING_SMEM, int MINB, bool TWO>
 __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel(KernelParams P) {
-  __shared__ GroupSmem s_grp[GROUPS];
+  constexpr int MS = TWO ? kMaxScope2p : kMaxScope;
+  __shared__ GroupSmem<MS> s_grp[GROUPS];
   extern __shared__ __align__(16) int32_t s_ring_dyn[];
   const int gib = threadIdx.x / (32 * G);
-  GroupSmem& S = s_grp[gib];
+  GroupSmem<MS>& S = s_grp[gib];
   Grp<G> g;
   g.tid = threadIdx.x % (32 * G);
   g.bar = 1 + gib;
@@ -1143,7 +1147,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
   fc.o2 = P.o2; fc.e2 = P.e2;
   fc.rdesc = S.rdesc[0]; fc.rdesc2 = rdesc2; fc.rphys = S.rphys[0]; fc.rdata = ring;
   DirCfg rc = fc;
-  rc.rdesc = S.rdesc[1]; rc.rdesc2 = rdesc2 + kMaxScope * 2; rc.rphys = S.rphys[1]; rc.rdata = ring + ring_dir;
+  rc.rdesc = S.rdesc[1]; rc.rdesc2 = rdesc2 + kMaxScope2p * 2; rc.rphys = S.rphys[1]; rc.rdata = ring + ring_dir;
   DirCfg bcfg{};
   bcfg.leaf = 1; bcfg.scope = P.scope; bcfg.magic = magic; bcfg.W = 0; bcfg.nphys = 1; bcfg.lmax = P.leaf_max_score;
   bcfg.nc = nc; bcfg.o2 = P.o2; bcfg.e2 = P.e2;

@@ -89,6 +89,11 @@ struct KernelParams {
   int ring_nphys;
 };
 
+// Score scope caps (max(x, o+e[, o2+e2]) + 1 after the match transform): the ring descriptors
+// live in shared memory, sized for the cap of each kernel instantiation.
+#define WFG_MAX_SCOPE 32
+#define WFG_MAX_SCOPE_2P 64
+
 // Physical ring buffers a direction needs: scores that can hold a wavefront are multiples of
 // g = gcd(x, o+e, e), so any window of `scope` consecutive scores holds at most ceil(scope/g)
 // live wavefronts, and round-robin buffers of that count are never overwritten while needed.
@@ -112,8 +117,8 @@ struct ArenaLayout {
   int64_t runs_off, runs_bytes;     // run_cap uint32
   int64_t lruns_off, lruns_bytes;   // leaf_run_cap uint32
   int64_t stack_off, stack_bytes;   // stack_cap x 8 int32
-  int64_t rdesc2_off, rdesc2_bytes; // I2/D2 ring descriptors, 2 directions x 32 scores x 2 x int2
-                                    // (ncomp == 5 only)
+  int64_t rdesc2_off, rdesc2_bytes; // I2/D2 ring descriptors, 2 directions x WFG_MAX_SCOPE_2P
+                                    // scores x 2 x int2 (ncomp == 5 only)
   int64_t total;
 };
 
@@ -130,7 +135,9 @@ WFG_HD constexpr inline ArenaLayout wfg_arena_layout(int scope, int ring_w, int 
   L.runs_off = off; L.runs_bytes = wfg_align256((int64_t)run_cap * 4); off += L.runs_bytes;
   L.lruns_off = off; L.lruns_bytes = wfg_align256((int64_t)leaf_run_cap * 4); off += L.lruns_bytes;
   L.stack_off = off; L.stack_bytes = wfg_align256((int64_t)stack_cap * 8 * 4); off += L.stack_bytes;
-  L.rdesc2_off = off; L.rdesc2_bytes = ncomp == 5 ? wfg_align256((int64_t)2 * 32 * 2 * 8) : 0; off += L.rdesc2_bytes;
+  L.rdesc2_off = off;
+  L.rdesc2_bytes = ncomp == 5 ? wfg_align256((int64_t)2 * WFG_MAX_SCOPE_2P * 2 * 8) : 0;
+  off += L.rdesc2_bytes;
   L.total = off;
   return L;
 }

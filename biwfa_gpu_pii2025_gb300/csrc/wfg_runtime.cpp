@@ -339,8 +339,9 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     return WF_STATUS_UNSUPPORTED;
   }
   const IntPen p = internal_penalties(cfg);
-  if (p.scope > 32) {
-    c->err = "max_score_scope above 32 is not supported";
+  if (p.scope > (p.nc == 5 ? WFG_MAX_SCOPE_2P : WFG_MAX_SCOPE)) {
+    c->err = p.nc == 5 ? "max_score_scope above 64 is not supported (two-piece gap-affine)"
+                       : "max_score_scope above 32 is not supported";
     return WF_STATUS_UNSUPPORTED;
   }
   if ((int64_t)(c->max_sum + 16) * (int64_t)std::max(p.x, std::max(p.o + p.e, p.o2 + p.e2)) >= ((int64_t)1 << 26)) {

@@ -157,7 +157,9 @@ def make_ref_cases():
         add(f"{tag}_score_only", pen, True, gen(5, 24, 305), 3)
     # two-piece gap-affine (match, mismatch, o1, e1, o2, e2), including match < 0 and a second
     # piece cheaper to open than the first
-    for pen in ((0, 4, 6, 2, 24, 1), (0, 3, 4, 2, 12, 1), (-2, 3, 1, 2, 8, 1), (0, 4, 12, 1, 3, 4)):
+    # (the last two: score scopes of 52 and 42, above the three-component kernels' cap of 32)
+    for pen in ((0, 4, 6, 2, 24, 1), (0, 3, 4, 2, 12, 1), (-2, 3, 1, 2, 8, 1), (0, 4, 12, 1, 3, 4),
+                (-1, 4, 6, 2, 24, 1), (0, 4, 6, 2, 40, 1)):
         tag = "affine2p_" + "_".join(map(str, pen))
         add(f"{tag}_generated", pen, False, gen(1, 8, 401) + gen(3, 12, 403) + gen(2, 24, 402), 4)
         add(f"{tag}_edges", pen, False, edges + far[:2], 4)

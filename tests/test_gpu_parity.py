@@ -58,9 +58,9 @@ def test_gpu_matches_oracle_on_generated(batch_aligner, workload, n, seed):
 OTHER_METRICS = [(_capi.METRIC_EDIT, (0, 0, 0, 0)), (_capi.METRIC_INDEL, (0, 0, 0, 0)),
                  (_capi.METRIC_GAP_LINEAR, (0, 4, 2, 0)), (_capi.METRIC_GAP_LINEAR, (-3, 2, 3, 0)),
                  (_capi.METRIC_GAP_AFFINE_2P, (0, 4, 6, 2, 24, 1)), (_capi.METRIC_GAP_AFFINE_2P, (-2, 3, 1, 2, 8, 1)),
-                 (_capi.METRIC_GAP_AFFINE_2P, (0, 4, 12, 1, 3, 4))]
+                 (_capi.METRIC_GAP_AFFINE_2P, (0, 4, 12, 1, 3, 4)), (_capi.METRIC_GAP_AFFINE_2P, (-1, 4, 6, 2, 24, 1))]
 OTHER_IDS = ["edit", "indel", "gap_linear_0_4_2", "gap_linear_m3_2_3", "affine2p_0_4_6_2_24_1",
-             "affine2p_m2_3_1_2_8_1", "affine2p_0_4_12_1_3_4"]
+             "affine2p_m2_3_1_2_8_1", "affine2p_0_4_12_1_3_4", "affine2p_m1_4_6_2_24_1_scope52"]
 
 
 @pytest.mark.parametrize("metric,pen", OTHER_METRICS, ids=OTHER_IDS)
