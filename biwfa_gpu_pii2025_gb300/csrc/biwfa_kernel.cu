@@ -274,7 +274,7 @@ __device__ __noinline__ void dir_init_5(const DirCfg& c, int cbi) {
     // diagonal 0 of score 0 (physical buffer 0)
     c.rdata[(size_t)(cbi < 3 ? cbi : c.nphys * 3 + (cbi - 3)) * c.W] = 0;
   } else {
-    for (int ci = 0; ci < 5; ++ci) set_desc<1>(c, 0, ci, kAbsent, INT_MIN, 0, 0);
+    for (int ci = 0; ci < c.nc; ++ci) set_desc<1>(c, 0, ci, kAbsent, INT_MIN, 0, 0);
     set_desc<1>(c, 0, cbi, 0, 0, 0, 0);
     c.ldata[0] = 0;
   }
