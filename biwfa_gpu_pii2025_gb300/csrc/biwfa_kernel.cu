@@ -1111,10 +1111,10 @@ struct GroupSmem {
 // G warps per pair, GROUPS groups per block. RING_SMEM: the two rings of each group live
 // in dynamic shared memory (sized by the host for ring_w); otherwise in the warp arena.
 // TWO: the two-piece gap-affine distance (five wavefront components); the other distances
-// run in the TWO = false instantiation.
-template <int G, int GROUPS, bool RING_SMEM, int MINB, bool TWO>
+// run in the TWO = false instantiations. MS: the score scope cap (shared-memory ring
+// descriptors), 32 for the usual penalties and 64 for larger ones.
+template <int G, int GROUPS, bool RING_SMEM, int MINB, bool TWO, int MS>
 __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel(KernelParams P) {
-  constexpr int MS = TWO ? kMaxScope2p : kMaxScope;
   __shared__ GroupSmem<MS> s_grp[GROUPS];
   extern __shared__ __align__(16) int32_t s_ring_dyn[];
   const int gib = threadIdx.x / (32 * G);
@@ -1348,55 +1348,57 @@ __global__ void pack_pairs_kernel(int n, const uint8_t* __restrict__ ascii, Pair
 // ------------------------------------------------------------------ host launchers
 namespace {
 
-// Execution shapes: (warps per pair, groups per block, rings in shared memory), each in a
-// three-component and a five-component (two-piece gap-affine) instantiation.
-template <int G, int GROUPS, bool RS, int MINB, bool TWO>
+// Execution shapes: (warps per pair, groups per block, rings in shared memory), each in three
+// instantiations: three components with a score scope up to 32 (the usual penalties), three
+// components up to 64, and five components (two-piece gap-affine) up to 64.
+template <int G, int GROUPS, bool RS, int MINB, bool TWO, int MS>
 cudaError_t launch_shape(const KernelParams& p, int grid, cudaStream_t stream) {
   const size_t dyn = RS ? (size_t)GROUPS * 2 * (size_t)(p.ring_nphys > 0 ? p.ring_nphys : p.scope) * (TWO ? 5 : 3) *
                               (size_t)p.ring_w * sizeof(int32_t)
                         : 0;
   if (dyn > 0) {
-    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO>,
+    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO, MS>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
   }
-  biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO><<<grid, G * GROUPS * 32, dyn, stream>>>(p);
+  biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO, MS><<<grid, G * GROUPS * 32, dyn, stream>>>(p);
   return cudaGetLastError();
 }
 
-template <int G, int GROUPS, bool RS, int MINB, bool TWO>
+template <int G, int GROUPS, bool RS, int MINB, bool TWO, int MS>
 cudaError_t occupancy_of(size_t dyn, int* blocks_per_sm) {
   if (dyn > 0) {
-    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO>,
+    const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO, MS>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
   }
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO>,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm,
+                                                       biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO, MS>,
                                                        G * GROUPS * 32, dyn);
 }
 
-template <bool TWO>
+template <bool TWO, int MS>
 cudaError_t occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm) {
-  if (gw <= 1) return occupancy_of<1, 4, false, kMinBlocksPerSM, TWO>(0, blocks_per_sm);
+  if (gw <= 1) return occupancy_of<1, 4, false, kMinBlocksPerSM, TWO, MS>(0, blocks_per_sm);
   if (gw == 8) {
-    if (ring_in_smem) return occupancy_of<8, 1, true, 1, TWO>(dyn, blocks_per_sm);
-    return occupancy_of<8, 1, false, 2, TWO>(0, blocks_per_sm);
+    if (ring_in_smem) return occupancy_of<8, 1, true, 1, TWO, MS>(dyn, blocks_per_sm);
+    return occupancy_of<8, 1, false, 2, TWO, MS>(0, blocks_per_sm);
   }
-  if (ring_in_smem) return occupancy_of<4, 1, true, 1, TWO>(dyn, blocks_per_sm);
-  return occupancy_of<4, 1, false, 3, TWO>(0, blocks_per_sm);
+  if (ring_in_smem) return occupancy_of<4, 1, true, 1, TWO, MS>(dyn, blocks_per_sm);
+  return occupancy_of<4, 1, false, 3, TWO, MS>(0, blocks_per_sm);
 }
 
-template <bool TWO>
+template <bool TWO, int MS>
 cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) {
   const int gw = p.group_warps > 0 ? p.group_warps : 1;
-  if (gw == 1) return launch_shape<1, 4, false, kMinBlocksPerSM, TWO>(p, grid, stream);
+  if (gw == 1) return launch_shape<1, 4, false, kMinBlocksPerSM, TWO, MS>(p, grid, stream);
   if (gw == 8) {
-    if (p.ring_in_smem) return launch_shape<8, 1, true, 1, TWO>(p, grid, stream);
-    return launch_shape<8, 1, false, 2, TWO>(p, grid, stream);
+    if (p.ring_in_smem) return launch_shape<8, 1, true, 1, TWO, MS>(p, grid, stream);
+    return launch_shape<8, 1, false, 2, TWO, MS>(p, grid, stream);
   }
   if (gw == 4) {
-    if (p.ring_in_smem) return launch_shape<4, 1, true, 1, TWO>(p, grid, stream);
-    return launch_shape<4, 1, false, 3, TWO>(p, grid, stream);
+    if (p.ring_in_smem) return launch_shape<4, 1, true, 1, TWO, MS>(p, grid, stream);
+    return launch_shape<4, 1, false, 3, TWO, MS>(p, grid, stream);
   }
   return cudaErrorInvalidValue;
 }
@@ -1406,14 +1408,21 @@ cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) 
 int biwfa_warps_per_block() { return 4; }
 
 cudaError_t biwfa_occupancy(int* blocks_per_sm) {
-  return occupancy_of<1, 4, false, kMinBlocksPerSM, false>(0, blocks_per_sm);
+  return occupancy_of<1, 4, false, kMinBlocksPerSM, false, kMaxScope>(0, blocks_per_sm);
 }
 
-// Resident blocks per SM of a shape (dyn: its dynamic shared memory in bytes; two: the
-// two-piece gap-affine instantiation).
-cudaError_t biwfa_occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm, int two) {
-  return two ? occupancy_shape<true>(gw, ring_in_smem, dyn, blocks_per_sm)
-             : occupancy_shape<false>(gw, ring_in_smem, dyn, blocks_per_sm);
+// The kernel instantiation of a launch: 0 three components (scope <= 32), 1 three components
+// (scope <= 64), 2 two-piece gap-affine (scope <= 64).
+int biwfa_kernel_kind(int metric, int scope) {
+  return metric == kMetricAffine2p ? 2 : (scope > kMaxScope ? 1 : 0);
+}
+
+// Resident blocks per SM of a shape (dyn: its dynamic shared memory in bytes; kind: as
+// biwfa_kernel_kind).
+cudaError_t biwfa_occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm, int kind) {
+  if (kind == 2) return occupancy_shape<true, kMaxScope2p>(gw, ring_in_smem, dyn, blocks_per_sm);
+  if (kind == 1) return occupancy_shape<false, kMaxScope2p>(gw, ring_in_smem, dyn, blocks_per_sm);
+  return occupancy_shape<false, kMaxScope>(gw, ring_in_smem, dyn, blocks_per_sm);
 }
 
 // Groups (pairs in flight) per block of a shape.
@@ -1423,7 +1432,10 @@ int biwfa_groups_per_block(int group_warps, int ring_in_smem) {
 }
 
 cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream) {
-  return p.metric == kMetricAffine2p ? launch_kernel<true>(p, grid, stream) : launch_kernel<false>(p, grid, stream);
+  const int kind = biwfa_kernel_kind(p.metric, p.scope);
+  if (kind == 2) return launch_kernel<true, kMaxScope2p>(p, grid, stream);
+  if (kind == 1) return launch_kernel<false, kMaxScope2p>(p, grid, stream);
+  return launch_kernel<false, kMaxScope>(p, grid, stream);
 }
 
 cudaError_t launch_pack(int n, const uint8_t* ascii, PairDesc* pairs, uint32_t* words, int num_sms,

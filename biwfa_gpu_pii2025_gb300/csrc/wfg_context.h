@@ -66,7 +66,8 @@ constexpr int kNumCounters = kOutHeadIndex + 4;
 cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream);
 cudaError_t biwfa_occupancy(int* blocks_per_sm);
 cudaError_t biwfa_occupancy_shape(int group_warps, int ring_in_smem, size_t dyn_smem, int* blocks_per_sm,
-                                  int two_piece);
+                                  int kind);
+int biwfa_kernel_kind(int metric, int scope);
 int biwfa_warps_per_block();
 int biwfa_groups_per_block(int group_warps, int ring_in_smem);
 cudaError_t launch_pack(int n, const uint8_t* ascii, PairDesc* pairs, uint32_t* words, int num_sms,

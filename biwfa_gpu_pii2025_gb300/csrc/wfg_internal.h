@@ -90,7 +90,8 @@ struct KernelParams {
 };
 
 // Score scope caps (max(x, o+e[, o2+e2]) + 1 after the match transform): the ring descriptors
-// live in shared memory, sized for the cap of each kernel instantiation.
+// live in shared memory, sized for the cap of each kernel instantiation (32 for the usual
+// penalties; 64 for larger ones and for two-piece gap-affine).
 #define WFG_MAX_SCOPE 32
 #define WFG_MAX_SCOPE_2P 64
 

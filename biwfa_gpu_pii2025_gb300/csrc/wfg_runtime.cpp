@@ -305,7 +305,8 @@ void size_launch(const wfg_context* c, const IntPen& p, int pass, int ring_w_hin
 int64_t max_groups(const wfg_context* c, const IntPen& p, const Launch& l) {
   const size_t dyn = l.smem ? (size_t)2 * p.nphys * p.nc * (size_t)l.ring_w * sizeof(int32_t) : 0;
   int bps = 0;
-  if (biwfa_occupancy_shape(l.gw, l.smem, dyn, &bps, p.nc == 5) != cudaSuccess || bps < 1) {
+  if (biwfa_occupancy_shape(l.gw, l.smem, dyn, &bps, biwfa_kernel_kind(p.nc == 5 ? 4 : 0, p.scope)) != cudaSuccess ||
+      bps < 1) {
     (void)cudaGetLastError();
     bps = 1;
   }
@@ -339,9 +340,8 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     return WF_STATUS_UNSUPPORTED;
   }
   const IntPen p = internal_penalties(cfg);
-  if (p.scope > (p.nc == 5 ? WFG_MAX_SCOPE_2P : WFG_MAX_SCOPE)) {
-    c->err = p.nc == 5 ? "max_score_scope above 64 is not supported (two-piece gap-affine)"
-                       : "max_score_scope above 32 is not supported";
+  if (p.scope > WFG_MAX_SCOPE_2P) {
+    c->err = "max_score_scope above 64 is not supported";
     return WF_STATUS_UNSUPPORTED;
   }
   if ((int64_t)(c->max_sum + 16) * (int64_t)std::max(p.x, std::max(p.o + p.e, p.o2 + p.e2)) >= ((int64_t)1 << 26)) {

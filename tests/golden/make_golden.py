@@ -139,6 +139,13 @@ def make_ref_cases():
     for pen in [(0, 4, 6, 2), (0, 1, 2, 1), (0, 3, 1, 4), (0, 5, 3, 2), (-5, 1, 2, 1), (-2, 3, 1, 4)]:
         add(f"edge_{'_'.join(map(str, pen))}", pen, False, edges)
     add("edge_score_only", (0, 4, 6, 2), True, edges)
+    # penalties whose score scope exceeds 32 (41 for both: plain, and match < 0 after the
+    # transform), run by the scope-64 kernel instantiation
+    for pen in ((0, 20, 30, 10), (-4, 8, 12, 6)):
+        tag = "affine_scope41_" + "_".join(map(str, pen))
+        add(f"{tag}_generated", pen, False, gen(1, 8, 501) + gen(3, 12, 503) + gen(2, 24, 502))
+        add(f"{tag}_edges", pen, False, edges)
+        add(f"{tag}_score_only", pen, True, gen(5, 24, 505))
     # edit and indel distances: generated pairs, edge cases, and pairs of very different
     # lengths whose wavefronts exceed 1,000 diagonals (edit's exact pruning)
     rnd = random.Random(77)

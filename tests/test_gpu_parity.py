@@ -312,3 +312,15 @@ def test_full_size_workloads(batch_aligner, workload, n, sample):
                                                        threads=16, return_ops=True)
     bad = [j for j, i in enumerate(idx) if pkg.runs_to_ops(res.runs_of(i)) != ops[j] or res.scores[i] != scores[j]]
     assert not bad, f"{len(bad)} of {sample} sampled pairs differ"
+
+
+def test_scope_above_64_is_refused(batch_aligner):
+    """Penalties whose score scope exceeds every kernel instantiation's cap are refused with a
+    status and a message, not run with a wrong ring."""
+    b = pkg.PairBatch.from_lists(["ACGTACGT"], ["ACGAACGT"])
+    batch_aligner.upload(b)
+    with pytest.raises(RuntimeError, match="max_score_scope"):
+        batch_aligner.run((0, 4, 60, 10))
+    res = batch_aligner.align(b, penalties=(0, 20, 30, 10))  # scope 41: the scope-64 kernel
+    st, score, ops, _ = binding.oracle_align(b.pattern(0), b.text(0), (0, 20, 30, 10))
+    assert res.status[0] == 0 and pkg.runs_to_ops(res.runs_of(0)) == ops and res.scores[0] == score
