@@ -222,8 +222,8 @@ typedef struct wfg_context wfg_context_t;
  * penalties; gap-linear takes its indel penalty from gap_opening (match <= 0, mismatch > 0,
  * indel > 0); two-piece gap-affine reads (gap_opening, gap_extension) as the first piece and
  * (gap_opening2, gap_extension2) as the second. The score scope (max(x, o+e[, o2+e2]) + 1
- * after the match < 0 transform) may be at most 32, or 64 for two-piece gap-affine; larger
- * penalties are refused with WF_STATUS_UNSUPPORTED. */
+ * after the match < 0 transform) may be at most 64; larger penalties are refused with
+ * WF_STATUS_UNSUPPORTED. */
 typedef enum {
   WFG_METRIC_GAP_AFFINE = 0, WFG_METRIC_EDIT = 1, WFG_METRIC_INDEL = 2, WFG_METRIC_GAP_LINEAR = 3,
   WFG_METRIC_GAP_AFFINE_2P = 4
