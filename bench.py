@@ -441,6 +441,8 @@ def run_distances(args):
     cells = float((batch.plen.astype(np.float64) * batch.tlen).sum())
     sample = np.random.default_rng(7).permutation(n)[:200]
     for dname, (metric, pen) in DISTANCES.items():
+        if args.only and args.only not in dname:
+            continue
         times, retried = {}, {}
         for sched_name in ("sorted", "plain"):
             sched = SCHEDS[sched_name]
@@ -516,6 +518,7 @@ def main():
     ap.add_argument("--plain-only", action="store_true", help="time only the plain length-sorted path")
     ap.add_argument("--distances", action="store_true",
                     help="one line per distance (gap-affine, two-piece, gap-linear, edit, indel)")
+    ap.add_argument("--only", default="", help="with --distances: the distances whose name contains this text")
     ap.add_argument("--profile-sched", choices=sorted(SCHEDS), default=None,
                     help="no timing: upload the batch, run the schedule warmup + steps times and exit "
                          "(the command the ncu captures in profiles/ run)")
