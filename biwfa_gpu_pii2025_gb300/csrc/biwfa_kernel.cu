@@ -29,8 +29,8 @@ namespace {
 constexpr int32_t kNull = INT32_MIN / 2;   // WAVEFRONT_OFFSET_NULL
 constexpr int kAbsent = INT32_MAX;         // lo of a wavefront that does not exist
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kMaxScope = WFG_MAX_SCOPE;    // score scope cap of the three-component kernels
-constexpr int kMaxScope2p = WFG_MAX_SCOPE_2P;  // the same for two-piece gap-affine
+constexpr int kMaxScope = WFG_MAX_SCOPE;       // score scope cap of the usual kernels (32)
+constexpr int kMaxScope2p = WFG_MAX_SCOPE_2P;  // the cap of the large-scope and two-piece kernels (64)
 #ifndef WFG_G1_MIN_BLOCKS
 #define WFG_G1_MIN_BLOCKS 7
 #endif
