@@ -76,3 +76,38 @@ def test_oracle_batch_threads_agree_with_single():
     assert (s1 == s4).all()
     for i in range(0, b.n, 7):
         assert binding.oracle_align(b.pattern(i), b.text(i))[1] == s1[i]
+
+
+def test_oracle_matches_live_reference_on_random_penalties():
+    """Random penalty sets for every distance (match <= 0 included, two-piece openings on either
+    side of the first piece's), a few mutated pairs each, full CIGAR and score-only."""
+    if binding.build_ref() is None:
+        pytest.skip("WFA2-lib reference sources not mounted here")
+    rng = np.random.default_rng(2026)
+    for trial in range(300):
+        m = -int(rng.integers(0, 4))
+        x, o, e = int(rng.integers(1, 9)), int(rng.integers(0, 11)), int(rng.integers(1, 6))
+        sets = [(binding.METRIC_AFFINE, (m, x, o, e)),
+                (binding.METRIC_LINEAR, (m, x, int(rng.integers(1, 9)), 0)),
+                (binding.METRIC_AFFINE2P, (m, x, o, e, int(rng.integers(0, 30)), int(rng.integers(1, 6)))),
+                (binding.METRIC_EDIT, (0, 0, 0, 0)), (binding.METRIC_INDEL, (0, 0, 0, 0))]
+        n = int(rng.integers(1, 260 if trial % 10 else 1500))
+        p = "".join(rng.choice(list("ACGT"), n))
+        t = list(p)
+        for _ in range(int(rng.integers(0, 25))):
+            if not t:
+                break
+            pos = int(rng.integers(0, len(t)))
+            r = rng.random()
+            if r < 0.4:
+                t[pos] = str(rng.choice(list("ACGT")))
+            elif r < 0.7:
+                t.insert(pos, "".join(rng.choice(list("ACGT"), int(rng.integers(1, 12)))))
+            else:
+                del t[pos:pos + int(rng.integers(1, 12))]
+        t = "".join(t)
+        for metric, pen in sets:
+            for score_only in (False, True):
+                ref = binding.ref_align(p, t, pen, score_only, metric=metric)
+                st, score, ops, _ = binding.oracle_align(p, t, pen, score_only, metric=metric)
+                assert (st, score, ops) == (ref[0], ref[1], ref[2]), (p, t, pen, metric, score_only)
