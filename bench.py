@@ -24,6 +24,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -119,7 +120,8 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        # raw samples; the JSON line carries their summary
+        self.path = Path(tempfile.gettempdir()) / f"biwfa_clocks_bench_{os.getpid()}.csv"
 
     def start(self):
         try:
