@@ -19,8 +19,8 @@ WF_STATUS_UNATTAINABLE = -300
 WF_STATUS_UNSUPPORTED = -400
 WF_STATUS_DEVICE_ERROR = -500
 
-# enums
-GAP_AFFINE = 3
+# enums (distance_metric_t of wavefront/wavefront_penalties.h)
+INDEL, EDIT, GAP_LINEAR, GAP_AFFINE, GAP_AFFINE_2P = 0, 1, 2, 3, 4
 COMPUTE_SCORE, COMPUTE_ALIGNMENT = 0, 1
 ALIGNMENT_END2END, ALIGNMENT_ENDSFREE = 0, 1
 WF_HEURISTIC_NONE, WF_HEURISTIC_WFADAPTIVE = 0, 4

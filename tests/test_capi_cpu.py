@@ -133,3 +133,48 @@ def test_cigar_scorers_match_oracle_rescoring(metric, pen):
         else:
             got = lib.cigar_score_gap_affine2p(C.byref(cg), C.byref(_capi.Affine2pPenalties(*pen)))
         assert got == score, (metric, pen, ops)
+
+
+def _refusal_status(mutate) -> int:
+    """wavefront_align's status for a default BiWFA configuration changed by `mutate`; an
+    unsupported configuration answers before any device is touched."""
+    lib = pkg.load_library()
+    attr = _capi.AlignerAttr.from_buffer_copy(_capi.attr_default())
+    attr.memory_mode = _capi.WAVEFRONT_MEMORY_ULTRALOW
+    attr.heuristic.strategy = _capi.WF_HEURISTIC_NONE
+    mutate(attr)
+    wf = lib.wavefront_aligner_new(C.byref(attr))
+    assert wf
+    try:
+        return lib.wavefront_align(wf, b"ACGTACGT", 8, b"ACGAACGT", 8)
+    finally:
+        lib.wavefront_aligner_delete(wf)
+
+
+@pytest.mark.parametrize("case", ["affine_mismatch0", "affine_match_pos", "affine2p_e2_0", "affine2p_o2_neg",
+                                  "linear_indel0", "heuristic", "memory_high", "endsfree", "metric_unknown"])
+def test_wfa2_api_refuses_bad_configurations_without_a_gpu(case):
+    def mutate(a):
+        if case == "affine_mismatch0":
+            a.affine_penalties = _capi.AffinePenalties(0, 0, 6, 2)
+        elif case == "affine_match_pos":
+            a.affine_penalties = _capi.AffinePenalties(1, 4, 6, 2)
+        elif case == "affine2p_e2_0":
+            a.distance_metric = _capi.GAP_AFFINE_2P
+            a.affine2p_penalties = _capi.Affine2pPenalties(0, 4, 6, 2, 24, 0)
+        elif case == "affine2p_o2_neg":
+            a.distance_metric = _capi.GAP_AFFINE_2P
+            a.affine2p_penalties = _capi.Affine2pPenalties(0, 4, 6, 2, -1, 1)
+        elif case == "linear_indel0":
+            a.distance_metric = _capi.GAP_LINEAR
+            a.linear_penalties = _capi.LinearPenalties(0, 4, 0)
+        elif case == "heuristic":
+            a.heuristic.strategy = _capi.WF_HEURISTIC_WFADAPTIVE
+        elif case == "memory_high":
+            a.memory_mode = _capi.WAVEFRONT_MEMORY_HIGH
+        elif case == "endsfree":
+            a.alignment_form.span = _capi.ALIGNMENT_ENDSFREE
+            a.alignment_form.text_end_free = 2
+        else:
+            a.distance_metric = 9
+    assert _refusal_status(mutate) == _capi.WF_STATUS_UNSUPPORTED
