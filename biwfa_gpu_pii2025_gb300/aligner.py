@@ -333,18 +333,27 @@ class ScorePredictor:
 
 
 class WavefrontAligner:
-    """WFA2-lib's aligner API (wavefront_aligner_new / wavefront_align), BiWFA on the GPU."""
+    """WFA2-lib's aligner API (wavefront_aligner_new / wavefront_align), BiWFA on the GPU.
+
+    distance: _capi.GAP_AFFINE (default; match, mismatch, gap_opening, gap_extension),
+    _capi.GAP_AFFINE_2P (plus gap_opening2, gap_extension2), _capi.GAP_LINEAR (match, mismatch
+    and the indel penalty in gap_opening), _capi.EDIT or _capi.INDEL (penalties unused)."""
 
     def __init__(self, match=0, mismatch=4, gap_opening=6, gap_extension=2, score_only=False,
-                 memory_mode=_capi.WAVEFRONT_MEMORY_ULTRALOW, heuristic=_capi.WF_HEURISTIC_NONE):
+                 memory_mode=_capi.WAVEFRONT_MEMORY_ULTRALOW, heuristic=_capi.WF_HEURISTIC_NONE,
+                 distance=_capi.GAP_AFFINE, gap_opening2=24, gap_extension2=1):
         self.lib = _capi.load()
         attr = _capi.AlignerAttr.from_buffer_copy(_capi.attr_default())
-        attr.distance_metric = _capi.GAP_AFFINE
+        attr.distance_metric = distance
         attr.affine_penalties = _capi.AffinePenalties(match, mismatch, gap_opening, gap_extension)
+        attr.affine2p_penalties = _capi.Affine2pPenalties(match, mismatch, gap_opening, gap_extension, gap_opening2,
+                                                          gap_extension2)
+        attr.linear_penalties = _capi.LinearPenalties(match, mismatch, gap_opening)
         attr.memory_mode = memory_mode
         attr.heuristic.strategy = heuristic
         attr.alignment_scope = _capi.COMPUTE_SCORE if score_only else _capi.COMPUTE_ALIGNMENT
         self.attr = attr
+        self.distance = distance
         self.penalties = _capi.AffinePenalties(match, mismatch, gap_opening, gap_extension)
         self.wf = self.lib.wavefront_aligner_new(C.byref(attr))
         if not self.wf:
@@ -389,7 +398,15 @@ class WavefrontAligner:
         return buf.value.decode()
 
     def cigar_score(self) -> int:
-        return self.lib.cigar_score_gap_affine(self.wf.contents.cigar, C.byref(self.penalties))
+        """The CIGAR rescored as align_benchmark prints it for the aligner's distance."""
+        cg = self.wf.contents.cigar
+        if self.distance == _capi.GAP_AFFINE_2P:
+            return self.lib.cigar_score_gap_affine2p(cg, C.byref(self.attr.affine2p_penalties))
+        if self.distance == _capi.GAP_LINEAR:
+            return self.lib.cigar_score_gap_linear(cg, C.byref(self.attr.linear_penalties))
+        if self.distance in (_capi.EDIT, _capi.INDEL):
+            return self.lib.cigar_score_edit(cg)
+        return self.lib.cigar_score_gap_affine(cg, C.byref(self.penalties))
 
     def sam_cigar(self, show_mismatches=True) -> list[int]:
         buf = _u32p()

@@ -178,3 +178,24 @@ def test_wfa2_api_refuses_bad_configurations_without_a_gpu(case):
         else:
             a.distance_metric = 9
     assert _refusal_status(mutate) == _capi.WF_STATUS_UNSUPPORTED
+
+
+@pytest.mark.parametrize("distance", ["GAP_AFFINE", "GAP_AFFINE_2P", "GAP_LINEAR", "EDIT", "INDEL"])
+def test_python_wavefront_aligner_builds_every_distance(distance):
+    """The Python mirror of WFA2-lib's aligner accepts every distance; without a GPU a valid
+    configuration reaches the device check, an invalid one is refused first."""
+    al = pkg.WavefrontAligner(distance=getattr(_capi, distance))
+    try:
+        st = al.align("ACGTACGT", "ACGAACGT")
+        assert st in (0, _capi.WF_STATUS_DEVICE_ERROR)
+    finally:
+        al.close()
+    bad = pkg.WavefrontAligner(distance=getattr(_capi, distance), mismatch=0)
+    try:
+        st = bad.align("ACGT", "ACGA")
+        # edit and indel ignore the penalties
+        assert st == (_capi.WF_STATUS_UNSUPPORTED if distance not in ("EDIT", "INDEL") else st)
+        if distance not in ("EDIT", "INDEL"):
+            assert st == _capi.WF_STATUS_UNSUPPORTED
+    finally:
+        bad.close()
