@@ -193,9 +193,9 @@ def test_python_wavefront_aligner_builds_every_distance(distance):
     bad = pkg.WavefrontAligner(distance=getattr(_capi, distance), mismatch=0)
     try:
         st = bad.align("ACGT", "ACGA")
-        # edit and indel ignore the penalties
-        assert st == (_capi.WF_STATUS_UNSUPPORTED if distance not in ("EDIT", "INDEL") else st)
-        if distance not in ("EDIT", "INDEL"):
+        if distance in ("EDIT", "INDEL"):  # they ignore the penalties
+            assert st in (0, _capi.WF_STATUS_DEVICE_ERROR)
+        else:
             assert st == _capi.WF_STATUS_UNSUPPORTED
     finally:
         bad.close()
