@@ -347,3 +347,28 @@ def test_adaptive_ring_start_keeps_results_exact(batch_aligner):
     for i in range(0, b.n, 37):
         _, score, ops, _ = binding.oracle_align(b.pattern(i), b.text(i))
         assert pkg.runs_to_ops(outs[2].runs_of(i)) == ops and outs[2].scores[i] == (score if ops else 0)
+
+
+def test_gpu_matches_oracle_on_random_penalties(batch_aligner):
+    """Random penalty sets for every distance (gap-open 0 and match < 0 included, score scope
+    within 64) on mutated pairs: the GPU path against the oracle, full CIGAR and score-only."""
+    rng = np.random.default_rng(4242)
+    metrics = {0: _capi.METRIC_GAP_AFFINE, 1: _capi.METRIC_EDIT, 2: _capi.METRIC_INDEL, 3: _capi.METRIC_GAP_LINEAR,
+               4: _capi.METRIC_GAP_AFFINE_2P}
+    b = pkg.PairBatch.generate(5, 40, seed=43)
+    for trial in range(24):
+        m = -int(rng.integers(0, 3))
+        x, o, e = int(rng.integers(1, 7)), int(rng.integers(0, 9)), int(rng.integers(1, 4))
+        cands = [(0, (m, x, o, e)), (3, (m, x, int(rng.integers(1, 7)), 0)),
+                 (4, (m, x, o, e, int(rng.integers(0, 16)), int(rng.integers(1, 4)))), (1, (0, 0, 0, 0)),
+                 (2, (0, 0, 0, 0))]
+        om, pen = cands[trial % len(cands)]
+        for score_only in (False, True):
+            res = batch_aligner.align(b, penalties=pen, metric=metrics[om], score_only=score_only)
+            for i in range(b.n):
+                st, score, ops, _ = binding.oracle_align(b.pattern(i), b.text(i), pen, score_only, metric=om)
+                assert res.status[i] == st, (pen, om, i)
+                if score_only:
+                    assert res.scores[i] == score, (pen, om, i)
+                else:
+                    assert pkg.runs_to_ops(res.runs_of(i)) == ops and res.scores[i] == (score if ops else 0), (pen, om, i)
