@@ -9,9 +9,10 @@ in HBM, L2 flushed before every step (512 MiB write). The default workload is th
 pair equal mixture of the 1 kbp / 5 %, 150 bp / 2 % and uneven 100 bp-10 kbp / 1-10 %
 workloads (seeded). Prints one JSON line.
 
---impl reference times the reference's own CPU algorithm on this machine's host cores: the
-C restatement of WFA2-lib's BiWFA (the WFA2-lib sources are not present on the GPU machine, so
-the compiled reference cannot run there), all host threads, a bounded sample per step.
+--impl reference times the reference's own CPU algorithm on this machine's host cores: WFA2-lib's
+BiWFA itself, compiled on this machine from the unmodified copy of its sources in the git-ignored
+baseline/_ref/ (oracle/Makefile `ref`), one aligner per thread on all host threads, over a fixed
+seeded sample of the batch per step; where that copy is absent, the oracle's C restatement of it.
 
 With torchrun (N > 1) every rank aligns its own shard of pairs (pairs are independent; no
 collective on the data path); the step time is the maximum over ranks.
@@ -46,8 +47,8 @@ SEED = 20251203
 TRAIN_SEED = 99991  # held-out seed of the predictor's training pairs
 L2_FLUSH_BYTES = 512 << 20
 # The port's single-thread speed relative to the real WFA2-lib on the same pairs (identical
-# scores), measured where both build (x86, oracle/calibrate_vs_wfa2.py): WFA2-lib itself is
-# absent on the GPU machine, so the reported CPU baseline is the port.
+# scores), measured where both build (x86, oracle/calibrate_vs_wfa2.py); reported only when the
+# CPU baseline has to fall back to the port.
 PORT_CALIBRATION = {"port_speed_over_wfa2lib_median": {"mixture": 0.80, "1kbp_5pct": 1.08, "150bp_2pct": 1.15,
                                                         "uneven": 0.79},
                     "mixture_range": [0.71, 1.00],
@@ -187,28 +188,64 @@ def profile_traffic():
     return None, ""
 
 
-def cpu_baseline(batch, sample_seconds: float = 12.0, threads: int | None = None, metric: int = 0,
-                 penalties=PENALTIES):
-    """The oracle (C restatement of WFA2-lib BiWFA) on all host cores over a bounded sample."""
+# Pairs of the CPU sample per workload: the first m of a seeded permutation of the batch, the
+# same m in the --impl reference arm and in the cpu_baseline leg, so the two time identical work
+# (about 2-6 s of 16 host cores per pass).
+CPU_SAMPLE = {1: 10_000, 2: 262_144, 3: 16_384, 4: 32, 5: 65_536}
+
+
+def cpu_sample(batch, workload: int):
+    m = min(batch.n, CPU_SAMPLE.get(workload, 65_536))
+    idx = np.random.default_rng(99).permutation(batch.n)[:m]
+    return batch.subset(idx), m
+
+
+def cpu_time(sub, threads: int, penalties=PENALTIES, metric: int = 0):
+    """One timed pass of the CPU reference over a sample: the real WFA2-lib (built on this
+    machine from its unmodified sources) when present, else the oracle port. Returns (seconds,
+    kind, scores, status)."""
     from oracle import binding
+    if metric == 0 and binding.ref_lib() is not None:
+        secs, scores, status = binding.ref_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen, penalties,
+                                                      threads=threads)
+        return secs, "reference", scores, status
+    secs, scores, status = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen, penalties,
+                                                     threads=threads, metric=metric)
+    return secs, "port", scores, status
+
+
+CPU_NOTE = {"reference": "WFA2-lib v2.3 BiWFA itself (ultralow memory, heuristic none, full CIGAR), compiled on "
+                         "this machine from its unmodified sources with its release flags; one aligner per thread",
+            "port": "the oracle: a C restatement of WFA2-lib v2.3 BiWFA, bit-exact with it (WFA2-lib's sources "
+                    "were not present on this machine)"}
+
+
+def cpu_baseline(batch, workload: int = 5, threads: int | None = None, metric: int = 0, penalties=PENALTIES):
+    """The CPU reference on all host cores over the workload's fixed sample (one warm pass,
+    then the timed pass)."""
     threads = threads or os.cpu_count() or 1
-    n = batch.n
-    rng = np.random.default_rng(99)
-    order = rng.permutation(n)
-    # grow the sample until it takes about sample_seconds of wall time (or covers the batch)
-    m2 = min(n, max(threads * 16, 256))
-    while True:
-        sub = batch.subset(order[:m2])
-        secs, scores, status = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen,
-                                                         penalties, threads=threads, metric=metric)
-        if secs >= 0.5 * sample_seconds or m2 >= n:
-            break
-        m2 = int(min(n, m2 * max(2.0, min(8.0, sample_seconds / max(secs, 1e-3)))))
+    sub, m = cpu_sample(batch, workload)
+    cpu_time(sub, threads, penalties, metric)
+    secs, kind, _, _ = cpu_time(sub, threads, penalties, metric)
     cells = float((sub.plen.astype(np.float64) * sub.tlen).sum())
-    return {"value": m2 / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
-            "sample": f"{m2} pairs drawn uniformly (seed 99) from the same batch; {secs:.2f} s wall",
-            "gcups": cells / secs / 1e9,
-            "calibration": PORT_CALIBRATION}
+    out = {"value": m / secs, "unit": "pairs/s", "cores": threads, "kind": kind,
+           "sample": f"{m} pairs drawn uniformly (seed 99) from the same batch; {secs:.2f} s wall",
+           "gcups": cells / secs / 1e9, "implementation": CPU_NOTE[kind]}
+    if kind == "port":
+        out["calibration"] = PORT_CALIBRATION
+    return out
+
+
+def parity_check(batch, res, penalties=PENALTIES, metric: int = 0) -> dict:
+    """Every pair of the timed batch against the oracle (status, score and the whole operation
+    string), on all host threads, outside the timed region."""
+    from oracle import binding
+    against = "wfa2" if metric == 0 and binding.ref_lib() is not None else "oracle"
+    r = binding.check_batch(batch.seq, batch.p_off, batch.plen, batch.t_off, batch.tlen, res.scores, res.status,
+                            res.runs, res.run_off, res.run_len, penalties, metric=metric, against=against)
+    return {"checked": r["checked"], "mismatches": r["mismatches"], "first_bad": r["first_bad"],
+            "against": ("WFA2-lib v2.3 itself (ultralow BiWFA), every pair of the timed batch" if against == "wfa2"
+                        else "the oracle (C restatement of WFA2-lib v2.3 BiWFA), every pair of the timed batch")}
 
 
 def run_reference(args):
@@ -219,25 +256,13 @@ def run_reference(args):
     name, n_full = WORKLOADS[wl]
     n = args.pairs or n_full
     batch = make_batch(wl, n, 0)
-    from oracle import binding
-    binding.oracle_lib()
     threads = os.cpu_count() or 1
-    rng = np.random.default_rng(99)
-    # a bounded sample per step, sized from a calibration run
-    m = min(n, threads * 8)
-    order = rng.permutation(n)
-    sub = batch.subset(order[:m])
-    secs, _, _ = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen, PENALTIES,
-                                           threads=threads)
-    budget = max(60.0 / max(args.steps + args.warmup, 1), 2.0)
-    m = int(min(n, max(m, budget / max(secs / m, 1e-7))))
-    sub = batch.subset(order[:m])
+    sub, m = cpu_sample(batch, wl)
     for _ in range(args.warmup):
-        binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen, PENALTIES, threads=threads)
-    times = []
+        cpu_time(sub, threads)
+    times, kind = [], "port"
     for _ in range(args.steps):
-        secs, _, st = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen, PENALTIES,
-                                                threads=threads)
+        secs, kind, _, _ = cpu_time(sub, threads)
         times.append(secs)
     t = sum(times)
     value = m * args.steps / t
@@ -249,11 +274,10 @@ def run_reference(args):
             "config": {"workload": name, "num_pairs": n, "sample_pairs_per_step": m, "seed": SEED,
                        "penalties": list(PENALTIES)},
             "gcups": cells * args.steps / t / 1e9,
-            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": kind,
                              "sample": f"{m} pairs per step drawn uniformly (seed 99) from the batch"},
             "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "WFA2-lib C restatement (bit-exact with WFA2-lib v2.3) on all host threads; the "
-                    "WFA2-lib sources are not present on the GPU machine"}
+            "note": CPU_NOTE[kind] + "; all host threads, the same sample as the GPU run's cpu_baseline"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -317,6 +341,9 @@ def run_ours(args):
     name, n_full = WORKLOADS[wl]
     n = args.pairs or n_full
     al = pkg.BatchAligner(local if world > 1 else 0)
+    if args.ring_w0 is not None or args.ring_from_pred is not None:
+        al.set_ring_start(1024 if args.ring_w0 is None else args.ring_w0,
+                          True if args.ring_from_pred is None else bool(args.ring_from_pred))
     learned = not args.plain_only
     pred, learn_info = None, None
     if learned:
@@ -407,7 +434,9 @@ def run_ours(args):
                                  "CIGAR runs; see profiles/ for issue utilisation"},
             "clocks": clk, "gpu_launches": launches}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(batch)
+        line["cpu_baseline"] = cpu_baseline(batch, wl)
+        # the oracle as the checker (untimed): every pair of this step's batch, bit-exact
+        line["parity"] = parity_check(batch, res)
     al.close()
     dist.close()
     if rank == 0:
@@ -479,7 +508,7 @@ def run_distances(args):
                            "sched": "sorted persistent (value), plain batched (plain_value)",
                            "l2": "flushed before every step (512 MiB write)"}}
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(batch, sample_seconds=8.0, metric=metric, penalties=pen)
+            line["cpu_baseline"] = cpu_baseline(batch, wl, metric=metric, penalties=pen)
         print(json.dumps(line), flush=True)
     al.close()
     return 0
@@ -517,6 +546,10 @@ def main():
     ap.add_argument("--workload", type=int, default=5, choices=sorted(WORKLOADS))
     ap.add_argument("--pairs", type=int, default=0, help="override the workload's pair count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ring-w0", type=int, default=None,
+                    help="first-pass starting ring width (0: each pair's full width; default: the library's 1024)")
+    ap.add_argument("--ring-from-pred", type=int, default=None, choices=[0, 1],
+                    help="learned schedule: start each pair at its predicted width (default: the library's 1)")
     ap.add_argument("--plain-only", action="store_true", help="time only the plain length-sorted path")
     ap.add_argument("--distances", action="store_true",
                     help="one line per distance (gap-affine, two-piece, gap-linear, edit, indel)")

@@ -62,12 +62,17 @@ class PlotAttr(C.Structure):
     _fields_ = [("enabled", C.c_bool), ("resolution_points", C.c_int), ("align_level", C.c_int)]
 
 
+class Timer(C.Structure):  # profiler_timer_t: struct timespec, profiler_counter_t, accumulated
+    _fields_ = [("tv_sec", C.c_int64), ("tv_nsec", C.c_long), ("counter", C.c_uint64 * 4), ("moments", C.c_double * 4),
+                ("accumulated", C.c_uint64)]
+
+
 class System(C.Structure):
     _fields_ = [("max_alignment_steps", C.c_int), ("probe_interval_global", C.c_int),
                 ("probe_interval_compact", C.c_int), ("max_partial_compacts", C.c_uint64),
                 ("max_memory_compact", C.c_uint64), ("max_memory_resident", C.c_uint64),
                 ("max_memory_abort", C.c_uint64), ("verbose", C.c_int), ("check_alignment_correct", C.c_bool),
-                ("max_num_threads", C.c_int), ("min_offsets_per_thread", C.c_int)]
+                ("timer", Timer), ("max_num_threads", C.c_int), ("min_offsets_per_thread", C.c_int)]
 
 
 class AlignerAttr(C.Structure):
@@ -85,12 +90,21 @@ class Cigar(C.Structure):
 
 class AlignStatus(C.Structure):
     _fields_ = [("status", C.c_int), ("score", C.c_int), ("dropped", C.c_bool), ("num_null_steps", C.c_int),
-                ("memory_used", C.c_uint64)]
+                ("memory_used", C.c_uint64), ("wf_align_compute", C.c_void_p), ("wf_align_extend", C.c_void_p)]
 
 
-class Aligner(C.Structure):
-    _fields_ = [("align_status", AlignStatus), ("alignment_scope", C.c_int), ("alignment_form", AlignmentForm),
-                ("memory_mode", C.c_int), ("cigar", C.POINTER(Cigar)), ("impl", C.c_void_p)]
+class EndPos(C.Structure):
+    _fields_ = [("score", C.c_int), ("k", C.c_int), ("offset", C.c_int32)]
+
+
+class Aligner(C.Structure):  # wavefront_aligner_t, WFA2-lib's layout
+    _fields_ = [("align_mode", C.c_int), ("align_mode_tag", C.c_char_p), ("align_status", AlignStatus),
+                ("sequences_", C.c_uint64 * 13), ("alignment_scope", C.c_int), ("alignment_form", AlignmentForm),
+                ("penalties_", C.c_int32 * 21), ("heuristic", Heuristic), ("memory_mode", C.c_int),
+                ("wf_components_", C.c_uint64 * 12), ("component_begin", C.c_int), ("component_end", C.c_int),
+                ("alignment_end_pos", EndPos), ("bialigner", C.c_void_p), ("cigar", C.POINTER(Cigar)),
+                ("mm_allocator_own", C.c_bool), ("mm_allocator", C.c_void_p), ("wavefront_slab", C.c_void_p),
+                ("plot", C.c_void_p), ("system", System)]
 
 
 class Config(C.Structure):

@@ -31,7 +31,7 @@ struct AlignerImpl {
   std::vector<int> plen, tlen, scores, statuses;
 };
 
-AlignerImpl* impl_of(wavefront_aligner_t* wf) { return static_cast<AlignerImpl*>(wf->impl); }
+AlignerImpl* impl_of(wavefront_aligner_t* wf) { return static_cast<AlignerImpl*>(wf->bialigner); }
 
 void check_config(AlignerImpl* im) {
   const wavefront_aligner_attr_t& a = im->attr;
@@ -120,7 +120,7 @@ wavefront_aligner_attr_t wavefront_aligner_attr_default = {
     wavefront_memory_high,
     NULL,
     {false, 2000, 0},
-    {INT_MAX, 3000, 6000, 0, (uint64_t)-1, (uint64_t)-1, UINT64_MAX, 0, false, 1, 500},
+    {INT_MAX, 3000, 6000, 0, (uint64_t)-1, (uint64_t)-1, UINT64_MAX, 0, false, {}, 1, 500},
 };
 
 // The GPU context is created by the first alignment (device WFG_DEVICE, default 0), so an
@@ -131,10 +131,14 @@ wavefront_aligner_t* wavefront_aligner_new(wavefront_aligner_attr_t* attributes)
   im->attr = *attributes;
   check_config(im);
   wavefront_aligner_t* wf = (wavefront_aligner_t*)calloc(1, sizeof(wavefront_aligner_t));
-  wf->impl = im;
+  wf->bialigner = im;
+  wf->align_mode = attributes->memory_mode == wavefront_memory_ultralow ? 1 : 0;  // wf_align_biwfa / _regular
   wf->alignment_scope = attributes->alignment_scope;
   wf->alignment_form = attributes->alignment_form;
+  wf->heuristic = attributes->heuristic;
   wf->memory_mode = attributes->memory_mode;
+  wf->mm_allocator = attributes->mm_allocator;
+  wf->system = attributes->system;
   wf->cigar = (cigar_t*)calloc(1, sizeof(cigar_t));
   wf->cigar->score = INT32_MIN;
   wf->cigar->end_v = wf->cigar->end_h = -1;

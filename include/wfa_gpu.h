@@ -22,6 +22,7 @@
 
 #include <stdbool.h>
 #include <stdint.h>
+#include <time.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -92,7 +93,18 @@ typedef enum {
 } wavefront_memory_t;
 /* wavefront/wavefront_plot.h (attributes part) */
 typedef struct { bool enabled; int resolution_points; int align_level; } wavefront_plot_attr_t;
-/* wavefront/wavefront_attributes.h:74-99 (the profiler timer is not carried) */
+/* system/profiler_counter.h:42-51 and system/profiler_timer.h:59-65: carried so that the
+ * attribute structure below has WFA2-lib's size and field offsets (the timer is never read). */
+typedef struct {
+  uint64_t total; uint64_t samples; uint64_t min; uint64_t max;
+  double m_oldM; double m_newM; double m_oldS; double m_newS;
+} profiler_counter_t;
+typedef struct {
+  struct timespec begin_timer;
+  profiler_counter_t time_ns;
+  uint64_t accumulated;
+} profiler_timer_t;
+/* wavefront/wavefront_attributes.h:74-99 */
 typedef struct {
   int max_alignment_steps;
   int probe_interval_global;
@@ -103,6 +115,7 @@ typedef struct {
   uint64_t max_memory_abort;
   int verbose;
   bool check_alignment_correct;
+  profiler_timer_t timer;
   int max_num_threads;
   int min_offsets_per_thread;
 } alignment_system_t;
@@ -143,23 +156,44 @@ typedef struct {
   int cigar_length;
 } cigar_t;
 
-/* wavefront/wfa.h:61-70 (function pointers omitted) */
+struct wavefront_aligner_t;
+/* wavefront/wfa.h:61-70 (the two function pointers are never set here) */
 typedef struct {
   int status;
   int score;
   bool dropped;
   int num_null_steps;
   uint64_t memory_used;
+  void (*wf_align_compute)(struct wavefront_aligner_t* const, const int);
+  int (*wf_align_extend)(struct wavefront_aligner_t* const, const int);
 } wavefront_align_status_t;
 
-/* wavefront/wfa.h:82-112: the public fields WFA2-lib callers read. */
+/* wavefront/wfa.h:82-112, byte for byte on LP64 (x86-64, AArch64): the fields WFA2-lib callers
+ * read (align_status, alignment_scope, alignment_form, heuristic, memory_mode, cigar, system)
+ * sit at WFA2-lib's offsets, so code compiled against WFA2-lib's headers reads them here too.
+ * WFA2-lib's internal members that callers do not read are opaque byte regions of their size;
+ * the bialigner slot holds this library's private state. */
 typedef struct wavefront_aligner_t {
+  int align_mode;                     /* wavefront_align_mode_t: 1 (BiWFA) for ultralow memory */
+  char* align_mode_tag;
   wavefront_align_status_t align_status;
+  uint64_t sequences_[13];            /* wavefront_sequences_t (104 bytes) */
   alignment_scope_t alignment_scope;
   alignment_form_t alignment_form;
+  int32_t penalties_[21];             /* wavefront_penalties_t (84 bytes) */
+  wavefront_heuristic_t heuristic;
   wavefront_memory_t memory_mode;
+  uint64_t wf_components_[12];        /* wavefront_components_t (96 bytes) */
+  int component_begin;                /* affine2p_matrix_type: 0 (M) */
+  int component_end;
+  struct { int score; int k; int32_t offset; } alignment_end_pos;  /* wavefront_pos_t */
+  void* bialigner;                    /* private: this library's aligner state */
   cigar_t* cigar;
-  void* impl;             /* private: device context and settings */
+  bool mm_allocator_own;
+  void* mm_allocator;
+  void* wavefront_slab;
+  void* plot;
+  alignment_system_t system;
 } wavefront_aligner_t;
 
 /* ------------------------------------------------------------------ WFA2-lib subset */

@@ -1115,3 +1115,31 @@ double orc_biwfa_align_batch(int n, const char* pat, const int64_t* pat_off, con
   return orc_wfa_align_batch(ORC_METRIC_AFFINE, n, pat, pat_off, plen, txt, txt_off, tlen, match, mismatch, gap_open,
                              gap_ext, score_only, ops, ops_off, scores, status, ops_len, nthreads);
 }
+
+/* ---------------------------------------------------------------- whole-batch comparison */
+/* Compares each pair's operations ops[ops_off[i] .. ops_off[i] + ops_len[i]) (M/X/I/D bytes, as
+ * the batch functions above write them) with a run-length list runs[run_off[i] .. run_off[i] +
+ * run_len[i]) of uint32 (len << 4 | SAM op: 7 '=' -> M, 8 X, 1 I, 2 D; the GPU's output form).
+ * bad[i] = 1 where they differ. Returns the number of differing pairs. */
+int64_t orc_compare_runs(int n, const char* ops, const int64_t* ops_off, const int* ops_len, const uint32_t* runs,
+                         const int64_t* run_off, const int* run_len, uint8_t* bad) {
+  int64_t nbad = 0;
+  for (int i = 0; i < n; ++i) {
+    const char* o = ops + ops_off[i];
+    const int len = ops_len[i];
+    int pos = 0, ok = 1;
+    for (int r = 0; r < run_len[i] && ok; ++r) {
+      const uint32_t v = runs[run_off[i] + r];
+      const int op = (int)(v & 15u), rl = (int)(v >> 4);
+      const char ch = op == 7 ? 'M' : op == 8 ? 'X' : op == 1 ? 'I' : op == 2 ? 'D' : '?';
+      if (ch == '?' || rl <= 0 || pos + rl > len) { ok = 0; break; }
+      for (int k = 0; k < rl; ++k)
+        if (o[pos + k] != ch) { ok = 0; break; }
+      pos += rl;
+    }
+    if (pos != len) ok = 0;
+    bad[i] = (uint8_t)(ok ? 0 : 1);
+    nbad += ok ? 0 : 1;
+  }
+  return nbad;
+}

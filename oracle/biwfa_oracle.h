@@ -89,6 +89,12 @@ double orc_wfa_align_batch_pen(int metric, int n, const char* pat, const int64_t
                                int score_only, char* ops, const int64_t* ops_off,
                                int* scores, int* status, int* ops_len, int nthreads);
 
+/* Compares pair i's operations (ops[ops_off[i] ..], ops_len[i] bytes of M/X/I/D) with the
+ * run-length list runs[run_off[i] ..], run_len[i] uint32 of (len << 4 | SAM op 7 '=', 8 X, 1 I,
+ * 2 D). bad[i] = 1 where they differ; returns the number of differing pairs. */
+int64_t orc_compare_runs(int n, const char* ops, const int64_t* ops_off, const int* ops_len, const uint32_t* runs,
+                         const int64_t* run_off, const int* run_len, uint8_t* bad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -177,3 +177,68 @@ double ref_biwfa_batch_time(int n, const char* seq, const long long* p_off, cons
   wavefront_aligner_delete(wf);
   return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }
+
+/* The timed CPU baseline: n pairs on nthreads POSIX threads, static interleaved partition, ONE
+ * WFA2-lib aligner per thread reused across its pairs (align_benchmark's per-thread use,
+ * tools/align_benchmark/align_benchmark.c:521-551), BiWFA gap-affine, full CIGAR. Writes each
+ * pair's status, printed score (cigar_score_gap_affine, -1 for an empty CIGAR) and, when ops is
+ * not NULL, its operations to ops[ops_off[i] ..] (capacity plen + tlen + 1) with their count in
+ * ops_len[i]. Returns the wall-clock seconds of the align loops (threads started and joined
+ * inside). */
+#include <pthread.h>
+typedef struct {
+  int tid, nthreads, n;
+  const char* seq; const long long* p_off; const int* plen; const long long* t_off; const int* tlen;
+  int pen[4];
+  char* ops; const long long* ops_off;
+  int* scores; int* status; int* ops_len;
+} ref_job_t;
+
+static void* ref_batch_worker(void* arg) {
+  ref_job_t* j = (ref_job_t*)arg;
+  wavefront_aligner_attr_t attr = wavefront_aligner_attr_default;
+  attr.distance_metric = gap_affine;
+  attr.affine_penalties.match = j->pen[0];
+  attr.affine_penalties.mismatch = j->pen[1];
+  attr.affine_penalties.gap_opening = j->pen[2];
+  attr.affine_penalties.gap_extension = j->pen[3];
+  attr.memory_mode = wavefront_memory_ultralow;
+  attr.heuristic.strategy = wf_heuristic_none;
+  attr.alignment_scope = compute_alignment;
+  wavefront_aligner_t* const wf = wavefront_aligner_new(&attr);
+  affine_penalties_t pen = {j->pen[0], j->pen[1], j->pen[2], j->pen[3]};
+  for (int i = j->tid; i < j->n; i += j->nthreads) {
+    j->status[i] = wavefront_align(wf, j->seq + j->p_off[i], j->plen[i], j->seq + j->t_off[i], j->tlen[i]);
+    cigar_t* const cg = wf->cigar;
+    const int nops = cg->end_offset - cg->begin_offset;
+    j->scores[i] = nops > 0 ? cigar_score_gap_affine(cg, &pen) : -1;
+    if (j->ops != NULL) {
+      const int cap = j->plen[i] + j->tlen[i] + 1;
+      const int m = (nops > 0 && nops <= cap) ? nops : 0;
+      if (m > 0) memcpy(j->ops + j->ops_off[i], cg->operations + cg->begin_offset, (size_t)m);
+      j->ops_len[i] = m;
+    }
+  }
+  wavefront_aligner_delete(wf);
+  return NULL;
+}
+
+double ref_biwfa_align_batch_mt(int n, const char* seq, const long long* p_off, const int* plen,
+                                const long long* t_off, const int* tlen, const int pen4[4], int nthreads, char* ops,
+                                const long long* ops_off, int* scores, int* status, int* ops_len) {
+  if (nthreads < 1) nthreads = 1;
+  pthread_t th[256];
+  ref_job_t jobs[256];
+  if (nthreads > 256) nthreads = 256;
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  for (int t = 0; t < nthreads; ++t) {
+    ref_job_t jb = {t, nthreads, n, seq, p_off, plen, t_off, tlen, {pen4[0], pen4[1], pen4[2], pen4[3]},
+                    ops, ops_off, scores, status, ops_len};
+    jobs[t] = jb;
+    pthread_create(&th[t], NULL, ref_batch_worker, &jobs[t]);
+  }
+  for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}

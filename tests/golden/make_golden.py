@@ -1,4 +1,5 @@
-"""Regenerates the golden fixtures in this folder (run where the reference tree is mounted).
+"""Regenerates the golden fixtures in this folder (run where the reference project is present;
+WFA2_SRC names its WFA2-lib folder).
 
 1. wfa2_utest.json.gz — WFA2-lib's own test vectors for this path, read as text from
    WFA2-lib/tests/: the 305 input pairs (wfa.utest.seq) and the expected `score\\tCIGAR`
@@ -13,22 +14,29 @@
    every workload and on edge cases, for the gap-affine, edit, indel, gap-linear and two-piece
    gap-affine distances ("metric" 0, 1, 2, 3, 4), so the GPU tests can pin parity on the GPU machine where the
    reference is absent.
+3. wfa2_abi_layout.txt — sizeof / offsetof of the structures a drop-in must match byte for byte
+   (tests/cpp/abi_layout.c compiled against WFA2-lib's own headers), so the layout test runs
+   where those headers are absent.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  WFA2_SRC=<reference>/WFA2-lib python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
 import gzip
 import json
+import os
 import random
+import subprocess
 import sys
+import tempfile
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
 
-WFA2_TESTS = Path("/root/reference/WFA2-lib/tests")
+WFA2_DIR = Path(os.environ.get("WFA2_SRC", ""))
+WFA2_TESTS = WFA2_DIR / "tests"
 
 UTEST_SETS = {
     # name: (penalties (match, mismatch, gap_open, gap_ext), score_only)
@@ -176,6 +184,19 @@ def make_ref_cases():
                    "cases": cases}, f)
 
 
+def make_abi_layout():
+    """tests/cpp/abi_layout.c against WFA2-lib's headers -> wfa2_abi_layout.txt."""
+    with tempfile.TemporaryDirectory() as td:
+        exe = Path(td) / "abi_layout"
+        subprocess.run(["gcc", "-std=gnu11", "-DWITH_WFA2", "-I", str(WFA2_DIR), str(HERE.parent / "cpp" / "abi_layout.c"),
+                        "-o", str(exe)], check=True)
+        out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    (HERE / "wfa2_abi_layout.txt").write_text(out)
+
+
 if __name__ == "__main__":
+    if not (WFA2_TESTS / "wfa.utest.seq").exists():
+        sys.exit("set WFA2_SRC to the reference's WFA2-lib folder")
     make_utest()
     make_ref_cases()
+    make_abi_layout()

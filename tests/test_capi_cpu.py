@@ -16,7 +16,8 @@ ROOT = Path(__file__).resolve().parent.parent
 def declared_functions():
     text = (ROOT / "include" / "wfa_gpu.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = set(re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{]*\)\s*;", text))
+    # function declarations only: `name(args);`, not function-pointer members `ret (*name)(args);`
+    names = set(re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\((?!\s*\*)[^;{]*\)\s*;", text))
     return sorted(n for n in names if n not in {"if", "while", "for", "return", "sizeof"})
 
 

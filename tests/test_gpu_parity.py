@@ -299,19 +299,21 @@ def _check_properties(b, res, penalties=(0, 4, 6, 2)):
     assert not same.any()
 
 
-@pytest.mark.parametrize("workload,n,sample", [(1, 10_000, 10_000), (2, 1_000_000, 20_000), (3, 200_000, 2_000),
-                                               (4, 2_000, 16), (5, 1_000_000, 5_000)])
-def test_full_size_workloads(batch_aligner, workload, n, sample):
-    """Full-size workloads: every pair checked by properties; a seeded sample bit-exact vs the oracle."""
+@pytest.mark.parametrize("workload,n,checked", [(1, 10_000, 10_000), (2, 1_000_000, 1_000_000),
+                                                (3, 200_000, 200_000), (4, 2_000, 200), (5, 1_000_000, 1_000_000)])
+def test_full_size_workloads(batch_aligner, workload, n, checked):
+    """Full-size workloads: every pair checked by properties, and every pair (the long noisy
+    workload: a seeded 200 of its 2,000) bit-exact against the oracle on all host threads —
+    status, score and the whole operation string."""
     b = pkg.PairBatch.generate(workload, n, seed=5000 + workload)
     res = batch_aligner.align(b)
     _check_properties(b, res)
-    idx = np.sort(np.random.default_rng(workload).choice(n, size=sample, replace=False))
-    sub = b.subset(idx)
-    _, scores, status, ops = binding.oracle_batch_time(sub.seq, sub.p_off, sub.plen, sub.t_off, sub.tlen,
-                                                       threads=16, return_ops=True)
-    bad = [j for j, i in enumerate(idx) if pkg.runs_to_ops(res.runs_of(i)) != ops[j] or res.scores[i] != scores[j]]
-    assert not bad, f"{len(bad)} of {sample} sampled pairs differ"
+    idx = None if checked == n else np.sort(np.random.default_rng(workload).choice(n, size=checked, replace=False))
+    r = binding.check_batch(b.seq, b.p_off, b.plen, b.t_off, b.tlen, res.scores, res.status, res.runs, res.run_off,
+                            res.run_len, idx=idx)
+    print(f"workload {workload}: {r['checked']} pairs checked against the oracle, {r['mismatches']} mismatches")
+    assert r["checked"] == checked
+    assert r["mismatches"] == 0, f"{r['mismatches']} of {checked} pairs differ, first {r['first_bad']}"
 
 
 def test_scope_above_64_is_refused(batch_aligner):

@@ -111,3 +111,54 @@ def test_oracle_matches_live_reference_on_random_penalties():
                 ref = binding.ref_align(p, t, pen, score_only, metric=metric)
                 st, score, ops, _ = binding.oracle_align(p, t, pen, score_only, metric=metric)
                 assert (st, score, ops) == (ref[0], ref[1], ref[2]), (p, t, pen, metric, score_only)
+
+
+def _runs_of_ops(ops: bytes):
+    code = {ord("M"): 7, ord("X"): 8, ord("I"): 1, ord("D"): 2}
+    runs, j = [], 0
+    while j < len(ops):
+        e = j
+        while e < len(ops) and ops[e] == ops[j]:
+            e += 1
+        runs.append(((e - j) << 4) | code[ops[j]])
+        j = e
+    return runs
+
+
+def test_batch_checker_finds_a_planted_difference():
+    """The whole-batch checker the full-size GPU tests and the bench use: results rebuilt from
+    the oracle's own operations pass; one planted change (in a copy of those results, on the
+    CPU) is found and named."""
+    import biwfa_gpu_pii2025_gb300 as pkg
+    b = pkg.PairBatch.generate(5, 240, 3)
+    _, sc, st, (ops, off, ln) = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=4,
+                                                          return_ops="raw")
+    runs, roff, rlen = [], [], []
+    for i in range(b.n):
+        r = _runs_of_ops(ops[off[i]:off[i] + ln[i]].tobytes())
+        roff.append(len(runs)); rlen.append(len(r)); runs += r
+    runs = np.array(runs, np.uint32); roff = np.array(roff, np.int64); rlen = np.array(rlen, np.int32)
+    scores = np.where(ln > 0, sc, 0)
+    ok = binding.check_batch(b.seq, b.p_off, b.plen, b.t_off, b.tlen, scores, st, runs, roff, rlen, chunk=64)
+    assert ok["checked"] == b.n and ok["mismatches"] == 0
+    planted = runs.copy()
+    planted[roff[17]] += 16  # one more base in pair 17's first run
+    bad = binding.check_batch(b.seq, b.p_off, b.plen, b.t_off, b.tlen, scores, st, planted, roff, rlen)
+    assert bad["mismatches"] == 1 and bad["first_bad"] == [17]
+    s2 = scores.copy(); s2[5] -= 2
+    assert binding.check_batch(b.seq, b.p_off, b.plen, b.t_off, b.tlen, s2, st, runs, roff, rlen)["first_bad"] == [5]
+
+
+def test_wfa2_threaded_batch_matches_oracle():
+    """The timed CPU baseline (the real WFA2-lib, one aligner per thread) gives the oracle's
+    status, score and operations on every pair."""
+    if binding.ref_lib() is None:
+        pytest.skip("WFA2-lib not built here")
+    import biwfa_gpu_pii2025_gb300 as pkg
+    b = pkg.PairBatch.generate(5, 600, 8)
+    _, s1, t1, (o1, f1, l1) = binding.oracle_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=4,
+                                                        return_ops="raw")
+    _, s2, t2, (o2, f2, l2) = binding.ref_batch_time(b.seq, b.p_off, b.plen, b.t_off, b.tlen, threads=4,
+                                                     return_ops=True)
+    assert np.array_equal(s1, s2) and np.array_equal(t1, t2) and np.array_equal(l1, l2)
+    assert all(o1[f1[i]:f1[i] + l1[i]].tobytes() == o2[f2[i]:f2[i] + l2[i]].tobytes() for i in range(b.n))
