@@ -6,7 +6,7 @@
 // the inputs and outputs already; what they cannot provide is this library's scratch.
 // This entry point therefore keeps all of its scratch — per-pair descriptors, packed
 // sequences, the work queue and the per-warp BiWFA arenas — in one file-scope
-// __device__ array of fixed size (kScratchBytes below, 28 MiB). Every GPU that loads
+// __device__ array of fixed size (kScratchBytes below, at most 32 MiB). Every GPU that loads
 // the library holds that array until the process exits.
 //
 // Host code cannot use the array's name as a device address (it is a host-side
@@ -42,8 +42,12 @@ constexpr int kMaxPairLen = WFG_NOALLOC_MAX_PAIR_LEN;   // plen + tlen <= 1024
 constexpr int kMaxScope = 16;                           // max(o+e, x) + 1 after the match transform
 constexpr int kWarps = 16;                              // resident warps of the aligner launch
 constexpr int kRingW = 2048;                            // >= kMaxPairLen + 8, power of two
-constexpr int kLeafWords = 1 << 16;
-constexpr int kLeafMaxScore = 1024;
+constexpr int kLeafWords = 1 << 17;                     // leaf offsets per warp (512 KiB)
+// Leaf descriptors for every score a unidirectional leaf can reach under any accepted
+// penalties (the batch path's bound, max(520, 100 x + o + 100 max(o, e) + scope) + 8, at its
+// largest for scope <= 16: x = 15, o = 14, e = 1). A leaf whose offsets outgrow kLeafWords
+// ends its pair with WF_STATUS_OOM (the batch path would finish it in a retry pass).
+constexpr int kLeafMaxScore = 15 * 100 + 14 + 14 * 100 + kMaxScope + 8;
 constexpr int kRunCap = kMaxPairLen + 2;
 constexpr int kStackCap = 64;
 // One fixed slot of packed words per pair: 2 x ((plen+3)/4 + 2) + 2 x ((tlen+3)/4 + 2).
@@ -56,7 +60,7 @@ constexpr int64_t kWordBytes = wfg_align256((int64_t)kMaxPairs * kWordsPerPair *
 constexpr int64_t kArenaBytes =
     wfg_arena_layout(kMaxScope, kRingW, kLeafMaxScore, kLeafWords, kRunCap, kRunCap, kStackCap).total;
 constexpr int64_t kScratchBytes = kHeaderBytes + kDescBytes + kOrderBytes + kWordBytes + kWarps * kArenaBytes;
-static_assert(kScratchBytes <= (int64_t)28 << 20, "no-alloc scratch above its stated 28 MiB");
+static_assert(kScratchBytes <= (int64_t)32 << 20, "no-alloc scratch above its stated 32 MiB");
 
 // The scratch. Device code may name it; host code must use its looked-up address.
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kScratchBytes];

@@ -416,7 +416,7 @@ int wfg_set_model(wfg_context_t* ctx, wfg_model_t* model);
  * that must not allocate while latency-critical work runs. The caller passes device
  * pointers to its inputs (sequence bytes, per-pair offsets and lengths) and to its
  * outputs (scores, statuses, run offsets and lengths, and a runs buffer of runs_cap
- * entries) and a cudaStream_t (or NULL); everything else lives in a fixed 28 MiB
+ * entries) and a cudaStream_t (or NULL); everything else lives in a fixed 30.7 MiB
  * __device__ array inside the library, held by every GPU that loads it until exit.
  * No cudaMalloc, cudaFree or other allocating call is made.
  *   - The first call on a device looks up that array's address (with that device
@@ -426,9 +426,15 @@ int wfg_set_model(wfg_context_t* ctx, wfg_model_t* model);
  *     is returned and nothing runs); pairs with plen + tlen above
  *     WFG_NOALLOC_MAX_PAIR_LEN get status WF_STATUS_UNSUPPORTED; penalties whose score
  *     scope max(o+e, x)+1 exceeds 16 are refused; a pair that outgrows the fixed arena
- *     gets WF_STATUS_OOM.
+ *     gets WF_STATUS_OOM: the arenas are sized like wfg_run's first pass, so a pair that
+ *     wfg_run finishes only in a retry pass (a unidirectional leaf of more than 131,072
+ *     offsets, e.g. a wide end-reached recovery leaf) comes back WF_STATUS_OOM here, never
+ *     with a different score or CIGAR.
+ *   - Throughput: one launch of 16 resident warps (one pair per warp at a time), so a call
+ *     suits modest batches; it is far below wfg_run's occupancy on large ones.
  * Returns WF_STATUS_ALG_COMPLETED once the work is enqueued on the stream; per-pair
- * results (same as wfg_run's) are valid after the stream completes. */
+ * results (the same as wfg_run's, up to the OOM case above) are valid after the stream
+ * completes. */
 #define WFG_NOALLOC_MAX_PAIRS 4096
 #define WFG_NOALLOC_MAX_PAIR_LEN 1024
 int wfg_align_noalloc(const wfg_config_t* cfg, int num_pairs, const char* d_seq,
