@@ -374,3 +374,30 @@ def test_gpu_matches_oracle_on_random_penalties(batch_aligner):
                     assert res.scores[i] == score, (pen, om, i)
                 else:
                     assert pkg.runs_to_ops(res.runs_of(i)) == ops and res.scores[i] == (score if ops else 0), (pen, om, i)
+
+
+@pytest.mark.parametrize("distance,pen,golden", [
+    (_capi.GAP_AFFINE_2P, (0, 4, 6, 2, 24, 1), "test.biwfa.affine2p.alg"),
+    (_capi.GAP_LINEAR, (0, 4, 2, 0), None),
+    (_capi.EDIT, (0, 0, 0, 0), "test.biwfa.edit.alg"),
+    (_capi.INDEL, (0, 0, 0, 0), "test.biwfa.indel.alg")], ids=["affine2p", "gap_linear", "edit", "indel"])
+def test_wfa2_single_pair_api_other_distances(distance, pen, golden):
+    """WFA2-lib's aligner API with the other distances: the operations and cigar_score() of
+    each pair equal the oracle's, and the printed `score\\tCIGAR` line equals WFA2-lib's own
+    golden line where WFA2-lib ships one."""
+    metric = {_capi.GAP_AFFINE_2P: binding.METRIC_AFFINE2P, _capi.GAP_LINEAR: binding.METRIC_LINEAR,
+              _capi.EDIT: binding.METRIC_EDIT, _capi.INDEL: binding.METRIC_INDEL}[distance]
+    data = utest()
+    o2, e2 = (pen[4], pen[5]) if len(pen) == 6 else (24, 1)
+    al = pkg.WavefrontAligner(*pen[:4], distance=distance, gap_opening2=o2, gap_extension2=e2)
+    try:
+        for i in (0, 3, 41, 150, 222, 304):
+            p, t = data["pairs"][i]
+            assert al.align(p, t) == _capi.WF_STATUS_ALG_COMPLETED
+            st, score, ops, _ = binding.oracle_align(p, t, pen, metric=metric)
+            assert st == 0 and al.cigar_ops() == ops, i
+            assert al.cigar_score() == score, i
+            if golden:
+                assert printed_line(al.cigar_score(), al.cigar_str()) == data["sets"][golden]["lines"][i], i
+    finally:
+        al.close()
