@@ -159,7 +159,6 @@ SIGNATURES = {
     "wfg_set_exec_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "wfg_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "wfg_set_retry_shape": (C.c_int, [C.c_void_p, C.c_int]),
-    "wfg_set_ring_start": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "wfg_set_learned_policy": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_float]),
     "wfg_autotune_learned_policy": (C.c_int, [C.c_void_p, P(Config), P(C.c_float), P(C.c_float), _ip, _ip]),
     "wfg_flush_l2": (C.c_int, [C.c_void_p, C.c_int64]),

@@ -191,11 +191,6 @@ class BatchAligner:
         """Warps per pair of the retry passes (default 8)."""
         self._check(self.lib.wfg_set_retry_shape(self.ctx, group_warps), "wfg_set_retry_shape")
 
-    def set_ring_start(self, ring_w0: int = 1024, from_prediction: bool = True):
-        """First-pass starting ring width (0: each pair's full width); pairs that outgrow it
-        restart in place at twice the width."""
-        self._check(self.lib.wfg_set_ring_start(self.ctx, ring_w0, 1 if from_prediction else 0), "wfg_set_ring_start")
-
     def set_learned_policy(self, wide_threshold=1200.0, wide_warps=8, wide_smem=True, ring_margin=1.4):
         self._check(self.lib.wfg_set_learned_policy(self.ctx, wide_threshold, wide_warps, 1 if wide_smem else 0,
                                                     ring_margin), "wfg_set_learned_policy")

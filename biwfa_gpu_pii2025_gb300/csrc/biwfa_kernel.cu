@@ -857,14 +857,14 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
     if (fmax + rmax >= max_antidiag) break;
     ++sf;
     const int qf = dir_step<G, 0, TWO>(F, p, sf, g, &ak);
-    if (qf < 0) return WFG_ST_RING_OVERFLOW;
+    if (qf < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (fmax < ak) fmax = ak;
     last_fwd = true;
     if (qf) return F.status;
     if (fmax + rmax >= max_antidiag) break;
     ++sr;
     const int qr = dir_step<G, 0, TWO>(R, p, sr, g, &ak);
-    if (qr < 0) return WFG_ST_RING_OVERFLOW;
+    if (qr < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (rmax < ak) rmax = ak;
     last_fwd = false;
     if (qr) return R.status;
@@ -878,7 +878,7 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
       overlap<G, TWO>(F, R, sf, sr, true, bp, p, g);
       ++sr;
       const int q = dir_step<G, 0, TWO>(R, p, sr, g, &ak);
-      if (q < 0) return WFG_ST_RING_OVERFLOW;
+      if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
       if (q) return R.status;
     }
     const int min_sf = (sf > p.scope - 1) ? sf - (p.scope - 1) : 0;
@@ -886,7 +886,7 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
     overlap<G, TWO>(R, F, sr, sf, false, bp, p, g);
     ++sf;
     const int q = dir_step<G, 0, TWO>(F, p, sf, g, &ak);
-    if (q < 0) return WFG_ST_RING_OVERFLOW;
+    if (q < 0) return WFG_ST_SCRATCH_OVERFLOW;
     if (q) return F.status;
     if (sr + sf >= max_steps) return WFG_ST_MAX_STEPS;
     if (sf > guard + 2 * p.scope || sr > guard + 2 * p.scope) return WFG_ST_UNATTAINABLE;
@@ -1177,35 +1177,21 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
     q.pr = q.tf + pd.tw_len;
     q.tr = q.pr + pd.pw_len;
     q.plen = pd.plen; q.tlen = pd.tlen; q.bshift = (pd.bits == 2) ? 1 : 3;
-    // Ring width of the pair. Every wavefront of the pair (and of its sub-windows) lies on
-    // diagonals [-plen-1, tlen+1], so next_pow2(plen+tlen+8) (within the slab's ring_w) never
-    // overflows; but wavefronts of low-error pairs stay far narrower, and a narrower ring
-    // spans less memory per warp, which measured markedly faster. So the pair starts at a
-    // smaller width (the launch's ring_w0, or the width its predicted score implies) and
-    // restarts in place at twice the width when a wavefront outgrows the ring. The two
-    // directions' rings are packed back to back at the width in use.
-    int wcap, wp;
     {
+      // Rings sized to the pair: every wavefront of the pair (and of its sub-windows) lies on
+      // diagonals [-plen-1, tlen+1], so a ring of next_pow2(plen+tlen+8) <= ring_w diagonals
+      // never overflows; the two directions' rings are packed back to back at that width
+      // (a smaller footprint per warp for short pairs).
       const uint32_t need = (uint32_t)(pd.plen + pd.tlen + 8);
-      wcap = min(P.ring_w, max(64, (int)(1u << (32 - __clz((int)need - 1)))));
-      int w0 = P.ring_w0 > 0 ? P.ring_w0 : wcap;
-      if (P.pred != nullptr) {
-        const float ps = fmaxf(P.pred[pi], 0.f) * P.pred_scale + 64.f;  // NaN becomes 64
-        const uint32_t pw = ps < 1.0e9f ? (uint32_t)ps : (1u << 30);
-        w0 = (int)(1u << (32 - __clz((int)max(pw, 64u) - 1)));
-      }
-      wp = min(wcap, max(64, w0));
+      const int wp = min(P.ring_w, max(64, (int)(1u << (32 - __clz((int)need - 1)))));
+      F.cfg.W = wp; R.cfg.W = wp;
+      F.cfg.rdata = ring;
+      R.cfg.rdata = ring + (size_t)nphys * nc * wp;
     }
     int status = ST_OK;
     int score = 0;
     int nsteps = 0, max_leaf = -1, max_depth = 0;
-    RunOut out;
-    for (;;) {  // restarts at twice the ring width
-    F.cfg.W = wp; R.cfg.W = wp;
-    F.cfg.rdata = ring;
-    R.cfg.rdata = ring + (size_t)nphys * nc * wp;
-    status = ST_OK; score = 0; max_leaf = -1; max_depth = 0;
-    out.buf = runs; out.n = 0; out.cap = P.run_cap; out.cur_op = -1; out.cur_len = 0; out.overflow = false;
+    RunOut out; out.buf = runs; out.n = 0; out.cap = P.run_cap; out.cur_op = -1; out.cur_len = 0; out.overflow = false;
 
     if (P.score_only) {
       // wavefront_bialign_compute_score (wavefront/wavefront_bialign.c:662-699)
@@ -1257,8 +1243,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
             } else {
               status = WFG_ST_UNATTAINABLE;
             }
-          } else if (st == WFG_ST_RING_OVERFLOW || st == WFG_ST_SCRATCH_OVERFLOW || st == WFG_ST_MAX_STEPS ||
-                     st == WFG_ST_OOM) {
+          } else if (st == WFG_ST_SCRATCH_OVERFLOW || st == WFG_ST_MAX_STEPS || st == WFG_ST_OOM) {
             status = st;
           } else {
             status = WFG_ST_UNATTAINABLE;
@@ -1294,14 +1279,6 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
         }
       }
     }
-    if (status == WFG_ST_RING_OVERFLOW && wp < wcap) {
-      wp = min(wcap, 2 * wp);
-      g.sync();
-      continue;
-    }
-    break;
-    }  // restart loop
-    if (status == WFG_ST_RING_OVERFLOW) status = WFG_ST_SCRATCH_OVERFLOW;  // at the slab's width
     if (status == WFG_ST_SCRATCH_OVERFLOW && P.retry_out != nullptr) {
       // Hand the pair to the next pass (larger arena); its results are written there.
       if (g.tid == 0) {

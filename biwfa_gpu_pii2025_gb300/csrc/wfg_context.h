@@ -142,8 +142,6 @@ struct wfg_context {
     int wide_smem = 1;
     float ring_margin = 1.4f;       // ring width = margin * predicted score / e + 64
     int retry_warps = 8;            // warps per pair in the retry passes (their pairs are wide)
-    int ring_w0 = 1024;             // first-pass starting ring width (0: each pair's full width)
-    int ring_from_pred = 1;         // learned schedule: start at the predicted width instead
   } tune;
   cudaStream_t aux_stream = nullptr;
   // wfg_run's device work as a CUDA graph (wfg_set_graph)

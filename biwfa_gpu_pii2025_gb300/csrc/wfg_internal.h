@@ -31,7 +31,6 @@ enum {
   WFG_ST_OOM = -200,              // WFA2's WF_STATUS_OOM
   WFG_ST_UNATTAINABLE = -300,
   WFG_ST_SCRATCH_OVERFLOW = -210, // the pair needs a larger per-warp arena (retried by the host)
-  WFG_ST_RING_OVERFLOW = -211,    // a wavefront outgrew the pair's ring width (restarted wider in place)
   WFG_ST_OUTPUT_OVERFLOW = -220,  // the dense output span could not be reserved
 };
 
@@ -88,13 +87,6 @@ struct KernelParams {
   int group_warps;
   int ring_in_smem;
   int ring_nphys;
-  // Adaptive ring width: a pair starts at ring_w0 diagonals (0: at its full width), or at the
-  // width its predicted score implies when pred is set (pred_scale = margin / cheapest gap
-  // base), and restarts in place at twice the width when a wavefront outgrows it, up to
-  // min(ring_w, next_pow2(plen + tlen + 8)).
-  int ring_w0;
-  const float* pred;
-  float pred_scale;
 };
 
 // Score scope caps (max(x, o+e[, o2+e2]) + 1 after the match transform): the ring descriptors

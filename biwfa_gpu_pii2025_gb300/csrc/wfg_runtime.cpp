@@ -505,10 +505,6 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     kp.group_warps = l.gw;
     kp.ring_in_smem = l.smem;
     kp.ring_nphys = p.nphys;
-    // adaptive ring width (first pass only: the retry passes hold pairs that outgrew it)
-    kp.ring_w0 = ps == 0 ? c->tune.ring_w0 : 0;
-    kp.pred = (ps == 0 && order_on_device && c->tune.ring_from_pred) ? c->d_pred.ptr : nullptr;
-    kp.pred_scale = (float)(c->tune.ring_margin / p.emin);
     kp.retry_out = (ps + 1 < kNumPasses) ? c->d_retry.ptr + (size_t)ps * n : nullptr;
     kp.retry_count = c->d_counters.ptr + ps * kCountersPerPass + 1;
     return kp;
@@ -628,13 +624,6 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
 int wfg_set_retry_shape(wfg_context_t* c, int group_warps) {
   if (!c || (group_warps != 1 && group_warps != 4 && group_warps != 8)) return WF_STATUS_UNSUPPORTED;
   c->tune.retry_warps = group_warps;
-  return WF_STATUS_ALG_COMPLETED;
-}
-
-int wfg_set_ring_start(wfg_context_t* c, int ring_w0, int from_prediction) {
-  if (!c || ring_w0 < 0) return WF_STATUS_UNSUPPORTED;
-  c->tune.ring_w0 = ring_w0;
-  c->tune.ring_from_pred = from_prediction ? 1 : 0;
   return WF_STATUS_ALG_COMPLETED;
 }
 

@@ -346,12 +346,6 @@ int wfg_set_graph(wfg_context_t* ctx, int enable);
 /* Warps per pair (1, 4 or 8, HBM rings) of the two retry passes, which realign the pairs that
  * overflowed the first pass's scratch: those are the widest pairs. Default 8. */
 int wfg_set_retry_shape(wfg_context_t* ctx, int group_warps);
-/* Starting ring width of the first pass: each pair starts with rings of ring_w0 diagonals (0:
- * the pair's full width, next_pow2(plen + tlen + 8) within the pass's cap), or, with
- * from_prediction set and WFG_SCHED_LEARNED, the width its predicted score implies; a pair
- * whose wavefront outgrows its ring restarts in place at twice the width. Results never
- * change. Defaults 1024 and 1. */
-int wfg_set_ring_start(wfg_context_t* ctx, int ring_w0, int from_prediction);
 /* Policy of WFG_SCHED_LEARNED: the pairs with the highest predicted scores, from
  * wide_threshold up and at most one resident wave of the shape, run with wide_warps warps per
  * pair (rings in shared memory when wide_smem and they fit), concurrently with the

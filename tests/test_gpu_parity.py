@@ -328,29 +328,6 @@ def test_scope_above_64_is_refused(batch_aligner):
     assert res.status[0] == 0 and pkg.runs_to_ops(res.runs_of(0)) == ops and res.scores[0] == score
 
 
-def test_adaptive_ring_start_keeps_results_exact(batch_aligner):
-    """Pairs that start with narrow rings and restart at twice the width (in place, as many
-    times as needed) give the results of pairs that start at their full width."""
-    b = pkg.PairBatch.generate(5, 600, seed=41)
-    outs = []
-    try:
-        for w0 in (0, 64, 256, 1024):
-            batch_aligner.set_ring_start(w0, False)
-            outs.append(batch_aligner.align(b))
-            outs.append(batch_aligner.align(b, penalties=(0, 4, 6, 2, 24, 1), metric=_capi.METRIC_GAP_AFFINE_2P))
-    finally:
-        batch_aligner.set_ring_start(1024, True)
-    for r in outs[2::2]:
-        assert np.array_equal(r.status, outs[0].status) and np.array_equal(r.scores, outs[0].scores)
-        assert np.array_equal(r.run_len, outs[0].run_len)
-    for r in outs[3::2]:
-        assert np.array_equal(r.status, outs[1].status) and np.array_equal(r.scores, outs[1].scores)
-        assert np.array_equal(r.run_len, outs[1].run_len)
-    for i in range(0, b.n, 37):
-        _, score, ops, _ = binding.oracle_align(b.pattern(i), b.text(i))
-        assert pkg.runs_to_ops(outs[2].runs_of(i)) == ops and outs[2].scores[i] == (score if ops else 0)
-
-
 def test_gpu_matches_oracle_on_random_penalties(batch_aligner):
     """Random penalty sets for every distance (gap-open 0 and match < 0 included, score scope
     within 64) on mutated pairs: the GPU path against the oracle, full CIGAR and score-only."""
