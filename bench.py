@@ -341,9 +341,6 @@ def run_ours(args):
     name, n_full = WORKLOADS[wl]
     n = args.pairs or n_full
     al = pkg.BatchAligner(local if world > 1 else 0)
-    if args.ring_w0 is not None or args.ring_from_pred is not None:
-        al.set_ring_start(1024 if args.ring_w0 is None else args.ring_w0,
-                          True if args.ring_from_pred is None else bool(args.ring_from_pred))
     learned = not args.plain_only
     pred, learn_info = None, None
     if learned:
@@ -546,10 +543,6 @@ def main():
     ap.add_argument("--workload", type=int, default=5, choices=sorted(WORKLOADS))
     ap.add_argument("--pairs", type=int, default=0, help="override the workload's pair count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ring-w0", type=int, default=None,
-                    help="first-pass starting ring width (0: each pair's full width; default: the library's 1024)")
-    ap.add_argument("--ring-from-pred", type=int, default=None, choices=[0, 1],
-                    help="learned schedule: start each pair at its predicted width (default: the library's 1)")
     ap.add_argument("--plain-only", action="store_true", help="time only the plain length-sorted path")
     ap.add_argument("--distances", action="store_true",
                     help="one line per distance (gap-affine, two-piece, gap-linear, edit, indel)")
