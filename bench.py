@@ -176,16 +176,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """Per-pair DRAM traffic of the alignment kernel from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "biwfa_kernel_traffic.json"
+def profile_counters():
+    """The alignment kernel's counters from the committed ncu summary, if any: DRAM traffic of
+    one launch and the integer-issue figures (issue-slot utilisation, long-scoreboard stalls,
+    local-memory instructions), with the workload and launch they were captured on."""
+    p = ROOT / "profiles" / "biwfa_kernel_counters.json"
     if p.exists():
         try:
-            d = json.loads(p.read_text())
-            return float(d["dram_bytes_per_pair"]), d.get("source", "")
+            return json.loads(p.read_text())
         except Exception:
-            return None, ""
-    return None, ""
+            return None
+    return None
 
 
 # Pairs of the CPU sample per workload: the first m of a seeded permutation of the batch, the
@@ -380,7 +381,12 @@ def run_ours(args):
     k_ms = statistics.mean(kernel_ms)
     achieved = alg_bytes / (k_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic_pp, _ = profile_traffic()
+    counters = profile_counters()
+    traffic = None
+    if counters and counters.get("pairs"):
+        # the capture's DRAM bytes per pair of its launch, times this launch's pairs (the same
+        # workload generator; the capture is one full launch when its pairs equal n)
+        traffic = float(counters["dram_bytes_read"] + counters["dram_bytes_write"]) / counters["pairs"] * n
 
     # ---- end to end through the public API with pinned host buffers
     pin = pkg.PinnedHost()
@@ -424,11 +430,16 @@ def run_ours(args):
                     "device_ms": statistics.mean(p[2] for p in parts)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": (traffic_pp * n) if traffic_pp else None,
+                         "traffic": traffic,
+                         "issue": ({k: counters[k] for k in ("issue_active_pct", "long_scoreboard_per_issue",
+                                                             "local_ld_per_launch", "local_st_per_launch",
+                                                             "warps_active_per_sm", "dram_throughput_pct",
+                                                             "pairs", "launch", "command") if k in counters}
+                                   if counters else None),
                          "kernel": "biwfa_persistent_kernel (3 passes)", "kernel_ms": k_ms,
                          "alg_bytes_per_launch": alg_bytes,
                          "note": "integer/latency-bound kernel: algorithmic bytes are 2-bit inputs + score + "
-                                 "CIGAR runs; see profiles/ for issue utilisation"},
+                                 "CIGAR runs; the issue figures (ncu, one launch) show the binding limit"},
             "clocks": clk, "gpu_launches": launches}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(batch, wl)

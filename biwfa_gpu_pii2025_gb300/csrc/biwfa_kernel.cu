@@ -95,51 +95,95 @@ struct SeqView {
   int bshift;
 };
 
+#ifndef WFG_SEQ_SMEM_WORDS
+#define WFG_SEQ_SMEM_WORDS 0
+#endif
+// Shared-memory words per single-warp group for its pair's packed sequences (0: none, the
+// default). A 2-bit pair whose four arrays fit is copied there (cp.async) when the group takes
+// it, and its windows are read from shared memory; other pairs read global memory. Measured on
+// the 1M-pair mixture (same GB300, identical results): 512 words 1.9 %, 768 words 1.6 % and
+// 1,280 words 6.9 % slower than global windows through the read-only path — the windows of a
+// pair mostly hit L1 already, the loads become generic, and the slots shrink L1.
+constexpr int kSeqSmemWords = WFG_SEQ_SMEM_WORDS;
+
+// One packed word. With shared-memory staging the pointer may address either space (a
+// generic load); otherwise global memory through the read-only path. The packed words are
+// read-only while the alignment kernel runs.
+__device__ __forceinline__ uint32_t seq_word(const uint32_t* w, uint32_t i) {
+  if (kSeqSmemWords > 0) return w[i];
+  return __ldg(w + i);
+}
+
 // 32-bit window of packed characters starting at character pos (first char in the low bits).
-// The packed words are read-only while the alignment kernel runs.
 __device__ __forceinline__ uint32_t win32(const uint32_t* w, int pos, int bshift) {
   const uint32_t bit = (uint32_t)pos << bshift;
   const uint32_t wi = bit >> 5;
-  return __funnelshift_r(__ldg(w + wi), __ldg(w + wi + 1), bit & 31u);
+  return __funnelshift_r(seq_word(w, wi), seq_word(w, wi + 1), bit & 31u);
+}
+
+// 64-bit window (32 bases of a 2-bit pair, 8 bytes of an 8-bit one) starting at character
+// pos: three words, two funnel shifts. Reads at most word (pos >> (5 - bshift)) + 2, inside
+// the array's two words of padding for every pos < the array's length.
+__device__ __forceinline__ uint64_t win64(const uint32_t* w, int pos, int bshift) {
+  const uint32_t bit = (uint32_t)pos << bshift;
+  const uint32_t wi = bit >> 5, sh = bit & 31u;
+  const uint32_t a = seq_word(w, wi), b = seq_word(w, wi + 1), c = seq_word(w, wi + 2);
+  return ((uint64_t)__funnelshift_r(b, c, sh) << 32) | __funnelshift_r(a, b, sh);
+}
+
+#ifndef WFG_LCP64
+#define WFG_LCP64 0
+#endif
+// Window of the LCP loop: 0 — 32-bit windows throughout (the default); 1 — the first window
+// 32-bit (most extensions of noisy pairs end inside it), the following ones 64-bit; 2 — 64-bit
+// throughout. Measured on the 1M-pair mixture (same GB300, identical results): 1 is 4 % and 2 is
+// 6 % slower than 0 — most extensions end within 16 bases, and the wider windows cost loads and
+// registers (the step's spills double).
+#if WFG_LCP64 == 2
+typedef uint64_t lcpw_t;
+#else
+typedef uint32_t lcpw_t;
+#endif
+
+__device__ __forceinline__ int first_set(uint32_t x) { return __ffs((int)x) - 1; }
+__device__ __forceinline__ int first_set(uint64_t x) { return __ffsll((long long)x) - 1; }
+
+// The LCP in two parts, so that the first windows of several diagonals load together:
+// lcp_first() is the XOR of the first windows (0 when nothing can match), lcp_rest()
+// continues from it.
+__device__ __forceinline__ lcpw_t lcp_first(const SeqView& s, int v, int h) {
+  if (min(s.plen - v, s.tlen - h) <= 0) return 0u;
+#if WFG_LCP64 == 2
+  return win64(s.pw, s.p0 + v, s.bshift) ^ win64(s.tw, s.t0 + h, s.bshift);
+#else
+  return win32(s.pw, s.p0 + v, s.bshift) ^ win32(s.tw, s.t0 + h, s.bshift);
+#endif
+}
+
+__device__ __forceinline__ int lcp_rest(const SeqView& s, int v, int h, lcpw_t x) {
+  const int maxn = min(s.plen - v, s.tlen - h);
+  if (maxn <= 0) return 0;
+  if (x) return min(first_set(x) >> s.bshift, maxn);
+  int n = (8 * (int)sizeof(lcpw_t)) >> s.bshift;
+#if WFG_LCP64 >= 1
+  const int cpw = 64 >> s.bshift;
+  for (; n < maxn; n += cpw) {
+    const uint64_t y = win64(s.pw, s.p0 + v + n, s.bshift) ^ win64(s.tw, s.t0 + h + n, s.bshift);
+    if (y) { n += first_set(y) >> s.bshift; break; }
+  }
+#else
+  const int cpw = 32 >> s.bshift;
+  for (; n < maxn; n += cpw) {
+    const uint32_t y = win32(s.pw, s.p0 + v + n, s.bshift) ^ win32(s.tw, s.t0 + h + n, s.bshift);
+    if (y) { n += first_set(y) >> s.bshift; break; }
+  }
+#endif
+  return min(n, maxn);
 }
 
 // Longest common extension of P[v..] and T[h..] inside the window: the sentinel-bounded
 // blockwise compare of wavefront_extend_matches_kernel_blockwise, with explicit bounds.
-__device__ __forceinline__ int lcp(const SeqView& s, int v, int h) {
-  const int maxn = min(s.plen - v, s.tlen - h);
-  if (maxn <= 0) return 0;
-  const int cpw = 32 >> s.bshift;
-  int n = 0;
-  for (;;) {
-    const uint32_t x = win32(s.pw, s.p0 + v + n, s.bshift) ^ win32(s.tw, s.t0 + h + n, s.bshift);
-    if (x) { n += (__ffs((int)x) - 1) >> s.bshift; break; }
-    n += cpw;
-    if (n >= maxn) break;
-  }
-  return min(n, maxn);
-}
-
-// lcp() split in two so that the first windows of several diagonals load together:
-// lcp_first() is the XOR of the first windows (0 when nothing can match), lcp_rest()
-// continues from it.
-__device__ __forceinline__ uint32_t lcp_first(const SeqView& s, int v, int h) {
-  if (min(s.plen - v, s.tlen - h) <= 0) return 0u;
-  return win32(s.pw, s.p0 + v, s.bshift) ^ win32(s.tw, s.t0 + h, s.bshift);
-}
-
-__device__ __forceinline__ int lcp_rest(const SeqView& s, int v, int h, uint32_t x) {
-  const int maxn = min(s.plen - v, s.tlen - h);
-  if (maxn <= 0) return 0;
-  const int cpw = 32 >> s.bshift;
-  int n = 0;
-  for (;;) {
-    if (x) { n += (__ffs((int)x) - 1) >> s.bshift; break; }
-    n += cpw;
-    if (n >= maxn) break;
-    x = win32(s.pw, s.p0 + v + n, s.bshift) ^ win32(s.tw, s.t0 + h + n, s.bshift);
-  }
-  return min(n, maxn);
-}
+__device__ __forceinline__ int lcp(const SeqView& s, int v, int h) { return lcp_rest(s, v, h, lcp_first(s, v, h)); }
 
 // A group of G warps that owns one pair. G == 1: warp-synchronous; G > 1: the warps meet
 // at named barrier `bar` (one per group in a block) and reduce through `red` (shared memory,
@@ -645,7 +689,7 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   constexpr int U = kLeaf ? kLeafUnroll : kStepUnroll;
   for (int kb = lo + g.tid; kb <= hi; kb += U * 32 * G) {
     int32_t mv[U], iv[U], dv[U];
-    uint32_t xw[U];
+    lcpw_t xw[U];
     #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int k = kb + u * 32 * G;
@@ -1177,6 +1221,29 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
     q.pr = q.tf + pd.tw_len;
     q.tr = q.pr + pd.pw_len;
     q.plen = pd.plen; q.tlen = pd.tlen; q.bshift = (pd.bits == 2) ? 1 : 3;
+    if (G == 1 && kSeqSmemWords > 0 && pd.bits == 2) {
+      // The four 2-bit arrays, each with the two words of padding the windows may read, into
+      // this group's shared-memory slot: [P fwd][T fwd][P rev][T rev]. The group's reads of
+      // the previous pair ended at its last group barrier.
+      const int pw2 = (pd.plen + 15) / 16 + 2, tw2 = (pd.tlen + 15) / 16 + 2;
+      if (2 * (pw2 + tw2) <= kSeqSmemWords) {
+        uint32_t* slot = reinterpret_cast<uint32_t*>(s_ring_dyn) + (size_t)gib * kSeqSmemWords;
+        const uint32_t* src[4] = {q.pf, q.tf, q.pr, q.tr};
+        const int len[4] = {pw2, tw2, pw2, tw2};
+        uint32_t* dst = slot;
+        #pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          for (int i = g.tid; i < len[a]; i += 32) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + i);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(src[a] + i) : "memory");
+          }
+          dst += len[a];
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncwarp();
+        q.pf = slot; q.tf = slot + pw2; q.pr = q.tf + tw2; q.tr = q.pr + pw2;
+      }
+    }
     {
       // Rings sized to the pair: every wavefront of the pair (and of its sub-windows) lies on
       // diagonals [-plen-1, tlen+1], so a ring of next_pow2(plen+tlen+8) <= ring_w diagonals
@@ -1351,11 +1418,14 @@ namespace {
 // Execution shapes: (warps per pair, groups per block, rings in shared memory), each in three
 // instantiations: three components with a score scope up to 32 (the usual penalties), three
 // components up to 64, and five components (two-piece gap-affine) up to 64.
+// Dynamic shared memory of the single-warp shape: the groups' packed-sequence slots.
+constexpr size_t kSeqSmemBytesG1 = (size_t)4 * kSeqSmemWords * sizeof(uint32_t);
+
 template <int G, int GROUPS, bool RS, int MINB, bool TWO, int MS>
 cudaError_t launch_shape(const KernelParams& p, int grid, cudaStream_t stream) {
   const size_t dyn = RS ? (size_t)GROUPS * 2 * (size_t)(p.ring_nphys > 0 ? p.ring_nphys : p.scope) * (TWO ? 5 : 3) *
                               (size_t)p.ring_w * sizeof(int32_t)
-                        : 0;
+                        : (G == 1 ? kSeqSmemBytesG1 : 0);
   if (dyn > 0) {
     const cudaError_t e = cudaFuncSetAttribute(biwfa_persistent_kernel<G, GROUPS, RS, MINB, TWO, MS>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
@@ -1379,7 +1449,7 @@ cudaError_t occupancy_of(size_t dyn, int* blocks_per_sm) {
 
 template <bool TWO, int MS>
 cudaError_t occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm) {
-  if (gw <= 1) return occupancy_of<1, 4, false, kMinBlocksPerSM, TWO, MS>(0, blocks_per_sm);
+  if (gw <= 1) return occupancy_of<1, 4, false, kMinBlocksPerSM, TWO, MS>(kSeqSmemBytesG1, blocks_per_sm);
   if (gw == 8) {
     if (ring_in_smem) return occupancy_of<8, 1, true, 1, TWO, MS>(dyn, blocks_per_sm);
     return occupancy_of<8, 1, false, 2, TWO, MS>(0, blocks_per_sm);
@@ -1408,7 +1478,7 @@ cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) 
 int biwfa_warps_per_block() { return 4; }
 
 cudaError_t biwfa_occupancy(int* blocks_per_sm) {
-  return occupancy_of<1, 4, false, kMinBlocksPerSM, false, kMaxScope>(0, blocks_per_sm);
+  return occupancy_of<1, 4, false, kMinBlocksPerSM, false, kMaxScope>(kSeqSmemBytesG1, blocks_per_sm);
 }
 
 // The kernel instantiation of a launch: 0 three components (scope <= 32), 1 three components
