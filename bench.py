@@ -404,7 +404,7 @@ def run_ours(args):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
         st = al.stats()
         h2d, d2h = st.h2d_bytes, st.d2h_bytes
-        parts.append((st.upload_host_ms, st.upload_copy_ms, st.total_ms))
+        parts.append((st.upload_host_ms, st.upload_copy_ms, st.total_ms, st.pipeline_chunks))
     e2e_t = dist.max(statistics.mean(e2e_ms))
     e2e_ok = bool(np.array_equal(out.scores[:n], res.scores)) and nruns == total_runs
     pin.close()
@@ -427,7 +427,10 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t, "matches_device_run": e2e_ok,
                     "upload_host_ms": statistics.mean(p[0] for p in parts),
                     "h2d_copy_ms": statistics.mean(p[1] for p in parts),
-                    "device_ms": statistics.mean(p[2] for p in parts)},
+                    "device_ms": statistics.mean(p[2] for p in parts),
+                    "pipeline_chunks": parts[-1][3],
+                    "note": "wfg_align_host: host->device copy of the inputs in chunks, overlapped with the "
+                            "alignment of the chunks already copied (pipeline_chunks 0: copy, then align)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": traffic,

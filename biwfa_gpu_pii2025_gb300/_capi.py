@@ -118,7 +118,7 @@ class Stats(C.Structure):
                 ("launches", C.c_int), ("retried_pairs", C.c_int), ("num_warps", C.c_int), ("ring_w", C.c_int),
                 ("arena_bytes", C.c_int64), ("total_runs", C.c_int64), ("h2d_bytes", C.c_int64),
                 ("d2h_bytes", C.c_int64), ("used_graph", C.c_int), ("upload_host_ms", C.c_double),
-                ("upload_copy_ms", C.c_double)]
+                ("upload_copy_ms", C.c_double), ("pipeline_chunks", C.c_int)]
 
 
 P = C.POINTER
@@ -158,6 +158,7 @@ SIGNATURES = {
     "wfg_set_arena_limits": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "wfg_set_exec_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "wfg_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "wfg_set_pipeline": (C.c_int, [C.c_void_p, C.c_int]),
     "wfg_set_retry_shape": (C.c_int, [C.c_void_p, C.c_int]),
     "wfg_set_learned_policy": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_float]),
     "wfg_autotune_learned_policy": (C.c_int, [C.c_void_p, P(Config), P(C.c_float), P(C.c_float), _ip, _ip]),

@@ -187,6 +187,10 @@ class BatchAligner:
         """Run each wfg_run's device work as one CUDA graph (default) or as direct launches."""
         self._check(self.lib.wfg_set_graph(self.ctx, 1 if enable else 0), "wfg_set_graph")
 
+    def set_pipeline(self, enable: bool = True):
+        """Let align_into (wfg_align_host) overlap its input copy with the alignment (default)."""
+        self._check(self.lib.wfg_set_pipeline(self.ctx, 1 if enable else 0), "wfg_set_pipeline")
+
     def set_retry_shape(self, group_warps: int = 8):
         """Warps per pair of the retry passes (default 8)."""
         self._check(self.lib.wfg_set_retry_shape(self.ctx, group_warps), "wfg_set_retry_shape")

@@ -110,9 +110,10 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(const int* __restrict__ 
 }
 
 __global__ void __launch_bounds__(kBinThreads) bin_scatter_kernel(int n, const float* __restrict__ pred,
-                                                                  int* __restrict__ cursor, int* __restrict__ order) {
+                                                                  int* __restrict__ cursor, int* __restrict__ order,
+                                                                  int base) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    order[atomicAdd(&cursor[bucket_of(pred[i])], 1)] = i;
+    order[atomicAdd(&cursor[bucket_of(pred[i])], 1)] = base + i;
 }
 
 }  // namespace
@@ -121,9 +122,10 @@ int sched_bin_words() { return 2 * kBuckets + 4; }
 
 // work: sched_bin_words() ints of scratch; stats (device, 4 ints) as bin_scan_kernel writes
 // them. wide_threshold: predicted score from which a pair may take the multi-warp launch;
-// wide_cap: at most that many pairs do (0 disables the wide launch).
+// wide_cap: at most that many pairs do (0 disables the wide launch). order receives base + i
+// for the n pairs pred[0..n) (base: the index of pred[0] in the batch).
 cudaError_t launch_bin_order(int n, const float* pred, float wide_threshold, int wide_cap, int* work, int* stats,
-                             int* order, int num_sms, cudaStream_t stream) {
+                             int* order, int num_sms, cudaStream_t stream, int base) {
   int* hist = work;
   int* cursor = work + kBuckets;
   cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(int) * kBuckets, stream);
@@ -140,7 +142,7 @@ cudaError_t launch_bin_order(int n, const float* pred, float wide_threshold, int
   if (blocks > num_sms * 4) blocks = num_sms * 4;
   bin_hist_kernel<<<blocks, kBinThreads, 0, stream>>>(n, pred, hist, stats);
   bin_scan_kernel<<<1, 1024, 0, stream>>>(hist, cursor, stats, n, wide_cap, wide_bucket);
-  bin_scatter_kernel<<<blocks, kBinThreads, 0, stream>>>(n, pred, cursor, order);
+  bin_scatter_kernel<<<blocks, kBinThreads, 0, stream>>>(n, pred, cursor, order, base);
   return cudaGetLastError();
 }
 

@@ -84,7 +84,7 @@ cudaError_t launch_mlp_adam(float* master, const float* grad, float* m, float* v
                             float eps, const int* step, void* w1t, void* w2t, cudaStream_t stream);
 int sched_bin_words();
 cudaError_t launch_bin_order(int n, const float* pred, float wide_threshold, int wide_cap, int* work, int* stats,
-                             int* order, int num_sms, cudaStream_t stream);
+                             int* order, int num_sms, cudaStream_t stream, int base = 0);
 cudaError_t launch_mlp_sync_bf16(const float* master, void* w1t, void* w2t, cudaStream_t stream);
 
 }  // namespace wfg
@@ -144,6 +144,10 @@ struct wfg_context {
     int retry_warps = 8;            // warps per pair in the retry passes (their pairs are wide)
   } tune;
   cudaStream_t aux_stream = nullptr;
+  // end-to-end pipeline (wfg_align_host): input copies on their own stream, per-chunk events
+  cudaStream_t copy_stream = nullptr;
+  int pipeline = 1;  // wfg_set_pipeline
+  std::vector<cudaEvent_t> chunk_ev;
   // wfg_run's device work as a CUDA graph (wfg_set_graph)
   int use_graph = 1;
   // timing of the last upload (wfg_get_stats)
@@ -154,6 +158,11 @@ struct wfg_context {
 };
 
 int wfg_fail(wfg_context* c, cudaError_t e, const char* where);
+int wfg_stage_pairs(wfg_context* c, int n, int64_t seq_len, const int64_t* p_off, const int* plen, const int64_t* t_off,
+                    const int* tlen);
+// Predicted scores of pairs [first, first + count) of the resident batch, features and MLP
+// forward on `stream` (wfg_model.cpp).
+int wfg_model_predict_range(wfg_model* m, wfg_context* c, int first, int count, cudaStream_t stream);
 #define WFG_CHECK(c, call)                                  \
   do {                                                      \
     cudaError_t _e = (call);                                \

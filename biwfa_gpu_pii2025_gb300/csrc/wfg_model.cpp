@@ -238,3 +238,15 @@ int wfg_set_model(wfg_context_t* c, wfg_model_t* m) {
 }
 
 }  // extern "C"
+
+int wfg_model_predict_range(wfg_model* m, wfg_context* c, int first, int count, cudaStream_t stream) {
+  if (!m || !c || first < 0 || count < 0 || first + count > c->n) return WF_STATUS_UNSUPPORTED;
+  if (count == 0) return WF_STATUS_ALG_COMPLETED;
+  WFG_CHECK(c, c->d_feats.reserve((size_t)std::max(c->n, 1) * kIn));
+  WFG_CHECK(c, c->d_pred.reserve((size_t)std::max(c->n, 1)));
+  uint16_t* feats = c->d_feats.ptr + (size_t)first * kIn;
+  WFG_CHECK(c, launch_kmer_features(count, c->d_seq.ptr, c->d_pairs.ptr + first, feats, c->num_sms, stream));
+  WFG_CHECK(c, launch_mlp_forward(count, feats, m->d_master.ptr, m->d_w1t.ptr, m->d_w2t.ptr, nullptr,
+                                  c->d_pred.ptr + first, c->num_sms, stream));
+  return WF_STATUS_ALG_COMPLETED;
+}

@@ -44,52 +44,11 @@ int wfg_fail(wfg_context* c, cudaError_t e, const char* where) {
   return WF_STATUS_DEVICE_ERROR;
 }
 
-extern "C" {
-
-wfg_context_t* wfg_context_create(int device) {
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return nullptr;
-  if (cudaSetDevice(device) != cudaSuccess) return nullptr;
-  wfg_context* c = new wfg_context();
-  c->device = device;
-  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking) != cudaSuccess) {
-    delete c;
-    return nullptr;
-  }
-  for (auto& e : c->ev) cudaEventCreate(&e);
-  if (c->d_counters.reserve(kNumCounters) != cudaSuccess || c->h_counters.reserve(kNumCounters) != cudaSuccess) {
-    delete c;
-    return nullptr;
-  }
-  return c;
-}
-
-void wfg_context_destroy(wfg_context_t* c) {
-  if (!c) return;
-  cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
-  c->d_seq.release(); c->d_pairs.release(); c->d_words.release(); c->d_order.release();
-  c->d_retry.release(); c->d_scores.release(); c->d_status.release(); c->d_runlen.release();
-  c->d_runoff.release(); c->d_runs.release(); c->d_counters.release(); c->d_arena.release();
-  c->d_flush.release(); c->h_counters.release(); c->h_pairs_pinned.release();
-  for (auto& e : c->ev) if (e) cudaEventDestroy(e);
-  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-  c->h_order_pin.release();
-  c->d_feats.release(); c->d_pred.release(); c->d_bin_work.release(); c->h_bin_stats.release();
-  c->d_batch_heads.release();
-  cudaStreamDestroy(c->stream);
-  cudaStreamDestroy(c->aux_stream);
-  delete c;
-}
-
-const char* wfg_last_error(wfg_context_t* c) { return c ? c->err.c_str() : "null context"; }
-
-int wfg_upload(wfg_context_t* c, int n, const char* seq, int64_t seq_len, const int64_t* p_off,
-               const int* plen, const int64_t* t_off, const int* tlen) {
-  if (!c || n < 0 || (n > 0 && (!seq || !p_off || !plen || !t_off || !tlen))) return WF_STATUS_UNSUPPORTED;
-  cudaSetDevice(c->device);
+// The host half of an upload: validates the pairs, builds their descriptors in the pinned
+// staging buffer and sizes the device buffers (no copy). The staging buffers are reused, so
+// every copy still reading them must be done first.
+int wfg_stage_pairs(wfg_context* c, int n, int64_t seq_len, const int64_t* p_off, const int* plen, const int64_t* t_off,
+                    const int* tlen) {
   const auto host_t0 = std::chrono::steady_clock::now();
   c->n = n;
   c->seq_len = seq_len;
@@ -99,7 +58,8 @@ int wfg_upload(wfg_context_t* c, int n, const char* seq, int64_t seq_len, const 
   c->feats_valid = c->pred_valid = false;
   c->max_plen = c->max_tlen = c->max_sum = 0;
   int64_t words = 0, out_cap = 0;
-  WFG_CHECK(c, cudaStreamSynchronize(c->stream));  // host staging buffers are reused below
+  WFG_CHECK(c, cudaStreamSynchronize(c->stream));
+  if (c->copy_stream) WFG_CHECK(c, cudaStreamSynchronize(c->copy_stream));
   WFG_CHECK(c, c->h_pairs_pinned.reserve((size_t)std::max(n, 1)));
   PairDesc* hp = c->h_pairs_pinned.ptr;
   for (int i = 0; i < n; ++i) {
@@ -138,9 +98,67 @@ int wfg_upload(wfg_context_t* c, int n, const char* seq, int64_t seq_len, const 
   WFG_CHECK(c, c->d_runoff.reserve((size_t)std::max(n, 1)));
   WFG_CHECK(c, c->d_runs.reserve((size_t)std::max<int64_t>(out_cap, 1)));
   c->upload_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+  return WF_STATUS_ALG_COMPLETED;
+}
+
+extern "C" {
+
+wfg_context_t* wfg_context_create(int device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+  wfg_context* c = new wfg_context();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return nullptr;
+  }
+  for (auto& e : c->ev) cudaEventCreate(&e);
+  if (c->d_counters.reserve(kNumCounters) != cudaSuccess || c->h_counters.reserve(kNumCounters) != cudaSuccess) {
+    delete c;
+    return nullptr;
+  }
+  return c;
+}
+
+void wfg_context_destroy(wfg_context_t* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->d_seq.release(); c->d_pairs.release(); c->d_words.release(); c->d_order.release();
+  c->d_retry.release(); c->d_scores.release(); c->d_status.release(); c->d_runlen.release();
+  c->d_runoff.release(); c->d_runs.release(); c->d_counters.release(); c->d_arena.release();
+  c->d_flush.release(); c->h_counters.release(); c->h_pairs_pinned.release();
+  for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  c->h_order_pin.release();
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
+  for (auto& e : c->chunk_ev) cudaEventDestroy(e);
+  c->d_feats.release(); c->d_pred.release(); c->d_bin_work.release(); c->h_bin_stats.release();
+  c->d_batch_heads.release();
+  cudaStreamDestroy(c->stream);
+  cudaStreamDestroy(c->aux_stream);
+  delete c;
+}
+
+const char* wfg_last_error(wfg_context_t* c) { return c ? c->err.c_str() : "null context"; }
+
+int wfg_upload(wfg_context_t* c, int n, const char* seq, int64_t seq_len, const int64_t* p_off,
+               const int* plen, const int64_t* t_off, const int* tlen) {
+  if (!c || n < 0 || (n > 0 && (!seq || !p_off || !plen || !t_off || !tlen))) return WF_STATUS_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  const int st = wfg_stage_pairs(c, n, seq_len, p_off, plen, t_off, tlen);
+  if (st != WF_STATUS_ALG_COMPLETED) return st;
   WFG_CHECK(c, cudaEventRecord(c->ev[6], c->stream));
   if (seq_len > 0) WFG_CHECK(c, cudaMemcpyAsync(c->d_seq.ptr, seq, (size_t)seq_len, cudaMemcpyHostToDevice, c->stream));
-  if (n > 0) WFG_CHECK(c, cudaMemcpyAsync(c->d_pairs.ptr, hp, sizeof(PairDesc) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  if (n > 0)
+    WFG_CHECK(c, cudaMemcpyAsync(c->d_pairs.ptr, c->h_pairs_pinned.ptr, sizeof(PairDesc) * (size_t)n,
+                                 cudaMemcpyHostToDevice, c->stream));
   WFG_CHECK(c, cudaEventRecord(c->ev[7], c->stream));
   c->uploaded = true;
   c->stats.h2d_bytes = seq_len + (int64_t)sizeof(PairDesc) * n;
@@ -313,12 +331,91 @@ int64_t max_groups(const wfg_context* c, const IntPen& p, const Launch& l) {
   return (int64_t)bps * c->num_sms * biwfa_groups_per_block(l.gw, l.smem);
 }
 
-}  // namespace
+// Kernel parameters of one launch of pass ps (0: first pass; the retry passes read the
+// previous pass's overflow list); the work queue (order, count, head) is set by the caller.
+KernelParams launch_params(const wfg_context* c, const wfg_config_t* cfg, const IntPen& p, const Launch& l, int ps) {
+  const int n = c->n;
+  KernelParams kp{};
+  kp.x = p.x; kp.o = p.o; kp.e = p.e; kp.scope = p.scope; kp.o2 = p.o2; kp.e2 = p.e2;
+  kp.match_o = cfg->match; kp.x_o = cfg->mismatch; kp.o_o = cfg->gap_opening; kp.e_o = cfg->gap_extension;
+  if (p.nc == 5) { kp.o2_o = cfg->gap_opening2; kp.e2_o = cfg->gap_extension2; }
+  kp.metric = cfg->metric;
+  kp.score_only = cfg->score_only;
+  kp.max_steps = cfg->max_alignment_steps > 0 ? cfg->max_alignment_steps : INT_MAX;
+  kp.pairs = c->d_pairs.ptr;
+  kp.words = c->d_words.ptr;
+  kp.arena = c->d_arena.ptr + l.arena_off;
+  kp.arena_bytes = l.L.total;
+  kp.ring_w = l.ring_w;
+  kp.leaf_words = l.leaf_words;
+  kp.leaf_max_score = l.leaf_max_score;
+  kp.run_cap = l.run_cap;
+  kp.leaf_run_cap = l.leaf_run_cap;
+  kp.stack_cap = l.stack_cap;
+  kp.scores = c->d_scores.ptr;
+  kp.status = c->d_status.ptr;
+  kp.run_off = c->d_runoff.ptr;
+  kp.run_len = c->d_runlen.ptr;
+  kp.out_runs = c->d_runs.ptr;
+  kp.out_cap = c->out_cap;
+  kp.out_head = c->d_counters.ptr + kOutHeadIndex;
+  kp.stats = nullptr;
+  kp.group_warps = l.gw;
+  kp.ring_in_smem = l.smem;
+  kp.ring_nphys = p.nphys;
+  kp.retry_out = (ps + 1 < kNumPasses) ? c->d_retry.ptr + (size_t)ps * n : nullptr;
+  kp.retry_count = c->d_counters.ptr + ps * kCountersPerPass + 1;
+  return kp;
+}
 
-extern "C" {
+// Shapes and arenas of the retry passes (1 .. kNumPasses-1), which realign the pairs that
+// overflowed the previous pass; returns the arena bytes the largest of them needs.
+int64_t plan_retry_passes(const wfg_context* c, const IntPen& p, int64_t arena_budget, Launch* retry) {
+  int64_t need = 0;
+  for (int ps = 1; ps < kNumPasses; ++ps) {
+    Launch& l = retry[ps];
+    l.gw = c->tune.retry_warps;  // pairs that overflowed the first pass are wide
+    size_launch(c, p, ps, 0, l);
+    const int gpb = biwfa_groups_per_block(l.gw, l.smem);
+    int64_t gmax = std::min<int64_t>(max_groups(c, p, l), std::max<int64_t>(gpb, (int64_t)c->n));
+    if (l.gw == 1) gmax = std::min<int64_t>(gmax, ps == 1 ? (int64_t)c->num_sms * 4 : (int64_t)c->num_sms * 2);
+    const int64_t fit = arena_budget / std::max<int64_t>(l.L.total, 1);
+    l.groups = std::max<int64_t>(gpb, (std::min(gmax, fit) / gpb) * gpb);
+    need = std::max(need, l.groups * l.L.total);
+  }
+  return need;
+}
 
-int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
-  if (!c || !cfg) return WF_STATUS_UNSUPPORTED;
+// Launch sizes of the first pass over `count` pairs with ring hint `hint` (0: the plain cap):
+// groups in flight within the device's residency and the arena budget.
+void plan_first_pass(const wfg_context* c, const IntPen& p, int hint, int64_t arena_budget, Launch& l) {
+  if (l.gw < 1) l.gw = 1;
+  if (l.gw != 1 && l.gw != 4 && l.gw != 8) l.gw = 8;
+  size_launch(c, p, 0, hint, l);
+  const int64_t gmax = std::min<int64_t>(max_groups(c, p, l), std::max<int64_t>(1, l.count));
+  const int64_t fit = arena_budget / std::max<int64_t>(l.L.total, 1);
+  l.groups = std::max<int64_t>(1, std::min(gmax, fit));
+  const int gpb = biwfa_groups_per_block(l.gw, l.smem);
+  l.groups = std::max<int64_t>(gpb, (l.groups / gpb) * gpb);
+}
+
+// The arena budget of a run: half of the device memory that is free or already held by the
+// arena, within [4 GiB, 96 GiB] (one GB300 has 288 GB of HBM).
+int64_t arena_budget_of(const wfg_context* c) {
+  int64_t budget = (int64_t)24 << 30;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+    const int64_t avail = (int64_t)free_b + (int64_t)c->d_arena.cap;
+    budget = std::min<int64_t>((int64_t)96 << 30, std::max<int64_t>((int64_t)4 << 30, avail / 2));
+  } else {
+    (void)cudaGetLastError();
+  }
+  return budget;
+}
+
+// The distance and penalties of a run, checked against the resident batch; *p receives the
+// internal penalties. Configuration errors are statuses with a message, never exits.
+int validate_config(wfg_context* c, const wfg_config_t* cfg, IntPen* p) {
   if (cfg->metric != WFG_METRIC_GAP_AFFINE && cfg->metric != WFG_METRIC_EDIT && cfg->metric != WFG_METRIC_INDEL &&
       cfg->metric != WFG_METRIC_GAP_LINEAR && cfg->metric != WFG_METRIC_GAP_AFFINE_2P) {
     c->err = "unknown distance metric";
@@ -339,15 +436,27 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     c->err = "two-piece penalties must satisfy match <= 0, mismatch > 0, o1 >= 0, e1 > 0, o2 >= 0, e2 > 0";
     return WF_STATUS_UNSUPPORTED;
   }
-  const IntPen p = internal_penalties(cfg);
-  if (p.scope > WFG_MAX_SCOPE_2P) {
+  *p = internal_penalties(cfg);
+  if (p->scope > WFG_MAX_SCOPE_2P) {
     c->err = "max_score_scope above 64 is not supported";
     return WF_STATUS_UNSUPPORTED;
   }
-  if ((int64_t)(c->max_sum + 16) * (int64_t)std::max(p.x, std::max(p.o + p.e, p.o2 + p.e2)) >= ((int64_t)1 << 26)) {
+  if ((int64_t)(c->max_sum + 16) * (int64_t)std::max(p->x, std::max(p->o + p->e, p->o2 + p->e2)) >= ((int64_t)1 << 26)) {
     c->err = "pair too long for 27-bit scores";
     return WF_STATUS_UNSUPPORTED;
   }
+  return WF_STATUS_ALG_COMPLETED;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
+  if (!c || !cfg) return WF_STATUS_UNSUPPORTED;
+  IntPen p;
+  const int vst = validate_config(c, cfg, &p);
+  if (vst != WF_STATUS_ALG_COMPLETED) return vst;
   cudaSetDevice(c->device);
   const int n = c->n;
   const int64_t h2d_upload = c->stats.h2d_bytes;
@@ -427,45 +536,16 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   }
   if (first.empty()) { Launch l; l.count = 0; first.push_back(l); }
   // ---- shapes and arena (pass-0 launches run concurrently; retry passes reuse the arena)
-  // Arena budget: half of the device memory that is free or already held by the arena, within
-  // [4 GiB, 96 GiB] (one GB300 has 288 GB of HBM).
-  int64_t arena_budget = (int64_t)24 << 30;
-  {
-    size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-      const int64_t avail = (int64_t)free_b + (int64_t)c->d_arena.cap;
-      arena_budget = std::min<int64_t>((int64_t)96 << 30, std::max<int64_t>((int64_t)4 << 30, avail / 2));
-    } else {
-      (void)cudaGetLastError();
-    }
-  }
+  const int64_t arena_budget = arena_budget_of(c);
   int64_t pass0_bytes = 0;
   for (Launch& l : first) {
-    if (l.gw < 1) l.gw = 1;
-    if (l.gw != 1 && l.gw != 4 && l.gw != 8) l.gw = 8;
     const int hint = l.ring_w > 0 ? l.ring_w : c->limit_ring_w;
-    size_launch(c, p, 0, hint, l);
-    int64_t gmax = std::min<int64_t>(max_groups(c, p, l), std::max<int64_t>(1, l.count));
-    const int64_t fit = (arena_budget / (int64_t)first.size()) / std::max<int64_t>(l.L.total, 1);
-    l.groups = std::max<int64_t>(1, std::min(gmax, fit));
-    const int gpb = biwfa_groups_per_block(l.gw, l.smem);
-    l.groups = std::max<int64_t>(gpb, (l.groups / gpb) * gpb);
+    plan_first_pass(c, p, hint, arena_budget / (int64_t)first.size(), l);
     l.arena_off = pass0_bytes;
     pass0_bytes += l.groups * l.L.total;
   }
   Launch retry[kNumPasses];
-  int64_t arena_need = pass0_bytes;
-  for (int ps = 1; ps < kNumPasses; ++ps) {
-    Launch& l = retry[ps];
-    l.gw = c->tune.retry_warps;  // pairs that overflowed the first pass are wide
-    size_launch(c, p, ps, 0, l);
-    const int gpb = biwfa_groups_per_block(l.gw, l.smem);
-    int64_t gmax = std::min<int64_t>(max_groups(c, p, l), std::max<int64_t>(gpb, (int64_t)n));
-    if (l.gw == 1) gmax = std::min<int64_t>(gmax, ps == 1 ? (int64_t)c->num_sms * 4 : (int64_t)c->num_sms * 2);
-    const int64_t fit = arena_budget / std::max<int64_t>(l.L.total, 1);
-    l.groups = std::max<int64_t>(gpb, (std::min(gmax, fit) / gpb) * gpb);
-    arena_need = std::max(arena_need, l.groups * l.L.total);
-  }
+  const int64_t arena_need = std::max(pass0_bytes, plan_retry_passes(c, p, arena_budget, retry));
   WFG_CHECK(c, c->d_arena.reserve((size_t)arena_need));
   int64_t num_batches = 0;
   for (const Launch& l : first)
@@ -476,39 +556,7 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
   if (c->ran) WFG_CHECK(c, cudaEventSynchronize(c->ev[0]));
   WFG_CHECK(c, c->h_order_pin.reserve((size_t)std::max(n, 1)));
   if (n > 0 && !order_on_device) std::copy(order.begin(), order.end(), c->h_order_pin.ptr);
-  auto params = [&](const Launch& l, int ps) {
-    KernelParams kp{};
-    kp.x = p.x; kp.o = p.o; kp.e = p.e; kp.scope = p.scope; kp.o2 = p.o2; kp.e2 = p.e2;
-    kp.match_o = cfg->match; kp.x_o = cfg->mismatch; kp.o_o = cfg->gap_opening; kp.e_o = cfg->gap_extension;
-    if (p.nc == 5) { kp.o2_o = cfg->gap_opening2; kp.e2_o = cfg->gap_extension2; }
-    kp.metric = cfg->metric;
-    kp.score_only = cfg->score_only;
-    kp.max_steps = cfg->max_alignment_steps > 0 ? cfg->max_alignment_steps : INT_MAX;
-    kp.pairs = c->d_pairs.ptr;
-    kp.words = c->d_words.ptr;
-    kp.arena = c->d_arena.ptr + l.arena_off;
-    kp.arena_bytes = l.L.total;
-    kp.ring_w = l.ring_w;
-    kp.leaf_words = l.leaf_words;
-    kp.leaf_max_score = l.leaf_max_score;
-    kp.run_cap = l.run_cap;
-    kp.leaf_run_cap = l.leaf_run_cap;
-    kp.stack_cap = l.stack_cap;
-    kp.scores = c->d_scores.ptr;
-    kp.status = c->d_status.ptr;
-    kp.run_off = c->d_runoff.ptr;
-    kp.run_len = c->d_runlen.ptr;
-    kp.out_runs = c->d_runs.ptr;
-    kp.out_cap = c->out_cap;
-    kp.out_head = c->d_counters.ptr + kOutHeadIndex;
-    kp.stats = nullptr;
-    kp.group_warps = l.gw;
-    kp.ring_in_smem = l.smem;
-    kp.ring_nphys = p.nphys;
-    kp.retry_out = (ps + 1 < kNumPasses) ? c->d_retry.ptr + (size_t)ps * n : nullptr;
-    kp.retry_count = c->d_counters.ptr + ps * kCountersPerPass + 1;
-    return kp;
-  };
+  auto params = [&](const Launch& l, int ps) { return launch_params(c, cfg, p, l, ps); };
   int launches = 0;
   // The device work of one run. Timing events are external record nodes when captured;
   // ev[5] / ev[4] fork the aux stream off and join it back (capture dependencies).
@@ -627,6 +675,12 @@ int wfg_set_retry_shape(wfg_context_t* c, int group_warps) {
   return WF_STATUS_ALG_COMPLETED;
 }
 
+int wfg_set_pipeline(wfg_context_t* c, int enable) {
+  if (!c) return WF_STATUS_UNSUPPORTED;
+  c->pipeline = enable ? 1 : 0;
+  return WF_STATUS_ALG_COMPLETED;
+}
+
 int wfg_set_graph(wfg_context_t* c, int enable) {
   if (!c) return WF_STATUS_UNSUPPORTED;
   c->use_graph = enable ? 1 : 0;
@@ -707,10 +761,198 @@ int wfg_fetch(wfg_context_t* c, int* scores, int* statuses, int64_t* run_off, in
   return WF_STATUS_ALG_COMPLETED;
 }
 
+}  // extern "C"
+
+namespace {
+
+constexpr int kPipelineMinPairs = 131072;  // batches from which wfg_align_host overlaps its input copy
+constexpr int kPipelinePairsPerChunk = 65536;
+constexpr int kPipelineMaxChunks = 8;
+
+// End-to-end alignment with the input copy overlapped with the alignment. The pairs are cut
+// into K chunks by index. The copy stream uploads the descriptors, then the sequence bytes up
+// to each chunk's last byte, chunk by chunk. As soon as chunk k's bytes are in, the aux stream
+// packs it and (learned schedule) computes its features, predictions and binned order; the main
+// stream then runs chunk k's first pass after chunk k-1's, while later chunks are still being
+// copied. The retry passes run once, over the overflows of every chunk. Scheduling only: every
+// pair's result is the one wfg_run gives.
+int align_host_pipelined(wfg_context* c, const wfg_config_t* cfg, wfg_sched_t sched, int n, const char* seq,
+                         int64_t seq_len, const int64_t* p_off, const int* plen, const int64_t* t_off, const int* tlen,
+                         int K) {
+  int st = wfg_stage_pairs(c, n, seq_len, p_off, plen, t_off, tlen);
+  if (st != WF_STATUS_ALG_COMPLETED) return st;
+  IntPen p;
+  st = validate_config(c, cfg, &p);
+  if (st != WF_STATUS_ALG_COMPLETED) return st;
+  const bool learned = sched == WFG_SCHED_LEARNED;
+  if (!c->copy_stream) WFG_CHECK(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  while ((int)c->chunk_ev.size() < 2 * K) {
+    cudaEvent_t e;
+    WFG_CHECK(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->chunk_ev.push_back(e);
+  }
+  // chunk k = pairs [cb[k], cb[k+1]); its bytes all lie below hi[k]
+  std::vector<int> cb((size_t)K + 1);
+  std::vector<int64_t> hi((size_t)K);
+  int64_t end = 0;
+  for (int k = 0; k < K; ++k) {
+    cb[(size_t)k] = (int)((int64_t)n * k / K);
+    cb[(size_t)k + 1] = (int)((int64_t)n * (k + 1) / K);
+    for (int i = cb[(size_t)k]; i < cb[(size_t)k + 1]; ++i)
+      end = std::max(end, std::max(p_off[i] + plen[i], t_off[i] + tlen[i]));
+    hi[(size_t)k] = end;
+  }
+  c->stats = wfg_stats_t{};
+  c->last_score_only = cfg->score_only;
+  c->stats.h2d_bytes = seq_len + (int64_t)sizeof(PairDesc) * n + (learned ? 0 : (int64_t)sizeof(int) * n);
+  // ---- host-side order of the sorted schedule: longest pairs first within each chunk
+  if (!learned) {
+    WFG_CHECK(c, c->h_order_pin.reserve((size_t)n));
+    std::vector<int> cnt((size_t)c->max_sum + 2);
+    for (int k = 0; k < K; ++k) {
+      std::fill(cnt.begin(), cnt.end(), 0);
+      const int a = cb[(size_t)k], b = cb[(size_t)k + 1];
+      for (int i = a; i < b; ++i) cnt[(size_t)(c->max_sum - (plen[i] + tlen[i])) + 1]++;
+      for (size_t v = 1; v < cnt.size(); ++v) cnt[v] += cnt[v - 1];
+      for (int i = a; i < b; ++i) c->h_order_pin.ptr[a + cnt[(size_t)(c->max_sum - (plen[i] + tlen[i]))]++] = i;
+    }
+  } else {
+    WFG_CHECK(c, c->d_pred.reserve((size_t)n));
+    WFG_CHECK(c, c->d_feats.reserve((size_t)n * WFG_MODEL_FEATURES));
+    WFG_CHECK(c, c->d_bin_work.reserve((size_t)sched_bin_words()));
+    WFG_CHECK(c, c->h_bin_stats.reserve((size_t)4 * K));
+  }
+  // ---- arena for the first pass at the plain ring cap and for the retry passes (a chunk whose
+  // predictions need wider rings grows it between chunks)
+  const int64_t budget = arena_budget_of(c);
+  Launch retry[kNumPasses];
+  int64_t arena_need = plan_retry_passes(c, p, budget, retry);
+  {
+    Launch l;
+    l.count = cb[1] - cb[0];
+    plan_first_pass(c, p, c->limit_ring_w, budget, l);
+    arena_need = std::max(arena_need, l.groups * l.L.total);
+  }
+  WFG_CHECK(c, c->d_arena.reserve((size_t)arena_need));
+  WFG_CHECK(c, c->d_batch_heads.reserve((size_t)K));
+  // ---- copies
+  cudaStream_t cs = c->copy_stream, ms = c->stream, as = c->aux_stream;
+  WFG_CHECK(c, cudaEventRecord(c->ev[6], cs));
+  WFG_CHECK(c, cudaMemcpyAsync(c->d_pairs.ptr, c->h_pairs_pinned.ptr, sizeof(PairDesc) * (size_t)n,
+                               cudaMemcpyHostToDevice, cs));
+  if (!learned)
+    WFG_CHECK(c, cudaMemcpyAsync(c->d_order.ptr, c->h_order_pin.ptr, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice,
+                                 cs));
+  int64_t lo = 0;
+  for (int k = 0; k < K; ++k) {
+    if (hi[(size_t)k] > lo)
+      WFG_CHECK(c, cudaMemcpyAsync(c->d_seq.ptr + lo, seq + lo, (size_t)(hi[(size_t)k] - lo), cudaMemcpyHostToDevice,
+                                   cs));
+    lo = std::max(lo, hi[(size_t)k]);
+    WFG_CHECK(c, cudaEventRecord(c->chunk_ev[(size_t)k], cs));
+  }
+  WFG_CHECK(c, cudaEventRecord(c->ev[7], cs));
+  // ---- main stream prologue
+  WFG_CHECK(c, cudaEventRecord(c->ev[0], ms));
+  WFG_CHECK(c, cudaEventRecord(c->ev[1], ms));
+  WFG_CHECK(c, cudaMemsetAsync(c->d_counters.ptr, 0, sizeof(unsigned long long) * kNumCounters, ms));
+  WFG_CHECK(c, cudaMemsetAsync(c->d_batch_heads.ptr, 0, sizeof(unsigned long long) * (size_t)K, ms));
+  WFG_CHECK(c, cudaEventRecord(c->ev[5], ms));
+  WFG_CHECK(c, cudaStreamWaitEvent(as, c->ev[5], 0));  // the aux stream's work follows this run's start
+  int launches = 0;
+  int64_t first_warps = 0;
+  int first_ring = 0;
+  int64_t first_arena = 0;
+  for (int k = 0; k < K; ++k) {
+    const int a = cb[(size_t)k], m = cb[(size_t)k + 1] - a;
+    cudaEvent_t ready = c->chunk_ev[(size_t)K + k];
+    // aux: pack, and for the learned schedule features, predictions and the chunk's order
+    WFG_CHECK(c, cudaStreamWaitEvent(as, c->chunk_ev[(size_t)k], 0));
+    WFG_CHECK(c, launch_pack(m, c->d_seq.ptr, c->d_pairs.ptr + a, c->d_words.ptr, c->num_sms, as));
+    ++launches;
+    if (learned) {
+      st = wfg_model_predict_range(c->model, c, a, m, as);
+      if (st != WF_STATUS_ALG_COMPLETED) return st;
+      int* stats = c->d_bin_work.ptr + sched_bin_words() - 4;
+      WFG_CHECK(c, launch_bin_order(m, c->d_pred.ptr + a, INFINITY, 0, c->d_bin_work.ptr, stats, c->d_order.ptr + a,
+                                    c->num_sms, as, a));
+      WFG_CHECK(c, cudaMemcpyAsync(c->h_bin_stats.ptr + 4 * k, stats, sizeof(int) * 4, cudaMemcpyDeviceToHost, as));
+      launches += 5;
+    }
+    WFG_CHECK(c, cudaEventRecord(ready, as));
+    // host: the chunk's ring width from its largest prediction (learned), then its first pass
+    Launch l;
+    l.count = m;
+    l.order_off = a;
+    int hint = c->limit_ring_w;
+    if (learned) {
+      WFG_CHECK(c, cudaEventSynchronize(ready));
+      float max_pred;
+      memcpy(&max_pred, &c->h_bin_stats.ptr[4 * k + 2], sizeof(float));
+      hint = (int)(c->tune.ring_margin * max_pred / p.emin) + 64;
+    }
+    plan_first_pass(c, p, hint, budget, l);
+    if ((size_t)(l.groups * l.L.total) > c->d_arena.cap) {
+      WFG_CHECK(c, cudaStreamSynchronize(ms));  // the earlier chunks' launches use the arena
+      WFG_CHECK(c, c->d_arena.reserve((size_t)(l.groups * l.L.total)));
+    }
+    WFG_CHECK(c, cudaStreamWaitEvent(ms, ready, 0));
+    KernelParams kp = launch_params(c, cfg, p, l, 0);
+    kp.num_pairs = m;
+    kp.num_pairs_ptr = nullptr;
+    kp.order = c->d_order.ptr + a;
+    kp.queue_head = c->d_batch_heads.ptr + k;
+    WFG_CHECK(c, launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), ms));
+    ++launches;
+    if (k == 0) { first_warps = l.groups * l.gw; first_ring = l.ring_w; first_arena = l.L.total; }
+  }
+  WFG_CHECK(c, cudaEventRecord(c->ev[2], ms));
+  for (int ps = 1; ps < kNumPasses; ++ps) {
+    const Launch& l = retry[ps];
+    KernelParams kp = launch_params(c, cfg, p, l, ps);
+    kp.num_pairs = n;
+    kp.num_pairs_ptr = c->d_counters.ptr + (ps - 1) * kCountersPerPass + 1;
+    kp.order = c->d_retry.ptr + (size_t)(ps - 1) * n;
+    kp.queue_head = c->d_counters.ptr + ps * kCountersPerPass + 0;
+    WFG_CHECK(c, launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), ms));
+    ++launches;
+  }
+  WFG_CHECK(c, cudaEventRecord(c->ev[3], ms));
+  WFG_CHECK(c, cudaMemcpyAsync(c->h_counters.ptr, c->d_counters.ptr, sizeof(unsigned long long) * kNumCounters,
+                               cudaMemcpyDeviceToHost, ms));
+  c->stats.used_graph = 0;
+  c->stats.launches = launches;
+  c->stats.num_warps = (int)first_warps;
+  c->stats.ring_w = first_ring;
+  c->stats.arena_bytes = first_arena;
+  c->stats.pipeline_chunks = K;
+  c->uploaded = true;
+  c->ran = true;
+  return WF_STATUS_ALG_COMPLETED;
+}
+
+}  // namespace
+
+extern "C" {
+
 int wfg_align_host(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched, int n, const char* seq,
                    int64_t seq_len, const int64_t* p_off, const int* plen, const int64_t* t_off, const int* tlen,
                    int* scores, int* statuses, int64_t* run_off, int* run_len, uint32_t* runs, int64_t runs_cap,
                    int64_t* total_runs) {
+  if (!c || !cfg || n < 0 || (n > 0 && (!seq || !p_off || !plen || !t_off || !tlen))) return WF_STATUS_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  // Large batches on the persistent schedules overlap the input copy with the alignment (the
+  // learned schedule with the context's model and a single-warp policy); the rest upload first.
+  const bool single_warp_policy = c->tune.wide_warps <= 1 || c->tune.wide_threshold >= 3.0e38f;
+  const bool pipelined = c->pipeline && n >= kPipelineMinPairs && c->force_gw == 1 && !c->force_smem &&
+                         (sched == WFG_SCHED_SORTED || (sched == WFG_SCHED_LEARNED && c->model != nullptr &&
+                                                        single_warp_policy));
+  if (pipelined) {
+    const int K = std::min(kPipelineMaxChunks, std::max(2, n / kPipelinePairsPerChunk));
+    const int st = align_host_pipelined(c, cfg, sched, n, seq, seq_len, p_off, plen, t_off, tlen, K);
+    if (st != WF_STATUS_ALG_COMPLETED) return st;
+    return wfg_fetch(c, scores, statuses, run_off, run_len, runs, runs_cap, total_runs);
+  }
   int st = wfg_upload(c, n, seq, seq_len, p_off, plen, t_off, tlen);
   if (st != WF_STATUS_ALG_COMPLETED) return st;
   st = wfg_run(c, cfg, sched);

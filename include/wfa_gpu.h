@@ -299,6 +299,8 @@ typedef struct {
   int used_graph;         /* 1 when the last wfg_run's device work ran as one CUDA graph */
   double upload_host_ms;  /* host time of the last wfg_upload before its copies (validation, descriptors) */
   double upload_copy_ms;  /* device time of the last wfg_upload's host-to-device copies */
+  int pipeline_chunks;    /* chunks of the last wfg_align_host whose input copy overlapped the
+                             alignment (0: uploaded first) */
 } wfg_stats_t;
 
 wfg_context_t* wfg_context_create(int device);
@@ -322,13 +324,21 @@ int wfg_run(wfg_context_t* ctx, const wfg_config_t* cfg, wfg_sched_t sched);
  * dense run buffer (runs_cap entries at most); run_off/run_len index into it. */
 int wfg_fetch(wfg_context_t* ctx, int* scores, int* statuses, int64_t* run_off, int* run_len,
               uint32_t* runs, int64_t runs_cap, int64_t* total_runs);
-/* Upload + run + fetch in one call (the end-to-end path). */
+/* Upload + run + fetch in one call (the end-to-end path). Batches of 131,072 pairs or more on
+ * WFG_SCHED_SORTED, or on WFG_SCHED_LEARNED with an attached model and a single-warp policy,
+ * overlap the input copy with the alignment: the pairs are cut into up to 8 chunks by index,
+ * and each chunk is packed, predicted, ordered and run (first pass) as soon as its bytes are
+ * on the device, while later chunks are still being copied; the retry passes run once at the
+ * end. This pays when the pairs' bytes lie in the buffer in pair order. Results are the same
+ * as upload + run + fetch. */
 int wfg_align_host(wfg_context_t* ctx, const wfg_config_t* cfg, wfg_sched_t sched,
                    int num_pairs, const char* seq, int64_t seq_len,
                    const int64_t* p_off, const int* plen, const int64_t* t_off, const int* tlen,
                    int* scores, int* statuses, int64_t* run_off, int* run_len,
                    uint32_t* runs, int64_t runs_cap, int64_t* total_runs);
 int wfg_get_stats(wfg_context_t* ctx, wfg_stats_t* stats);
+/* Whether wfg_align_host may overlap its input copy with the alignment (default 1). */
+int wfg_set_pipeline(wfg_context_t* ctx, int enable);
 /* Caps on the first pass's per-warp arena (0 = automatic): ring width in diagonals and
  * leaf store in int32 words. Pairs that do not fit overflow into the retry passes, whose
  * arenas are sized from the batch's longest pair; results never change. */
