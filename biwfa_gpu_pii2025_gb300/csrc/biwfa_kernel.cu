@@ -121,6 +121,14 @@ __device__ __forceinline__ uint32_t win32(const uint32_t* w, int pos, int bshift
   return __funnelshift_r(seq_word(w, wi), seq_word(w, wi + 1), bit & 31u);
 }
 
+#ifndef WFG_LCP64
+#define WFG_LCP64 0
+#endif
+#ifndef WFG_ALIGN_START
+#define WFG_ALIGN_START 0
+#endif
+
+#if WFG_LCP64 >= 1
 // 64-bit window (32 bases of a 2-bit pair, 8 bytes of an 8-bit one) starting at character
 // pos: three words, two funnel shifts. Reads at most word (pos >> (5 - bshift)) + 2, inside
 // the array's two words of padding for every pos < the array's length.
@@ -130,9 +138,7 @@ __device__ __forceinline__ uint64_t win64(const uint32_t* w, int pos, int bshift
   const uint32_t a = seq_word(w, wi), b = seq_word(w, wi + 1), c = seq_word(w, wi + 2);
   return ((uint64_t)__funnelshift_r(b, c, sh) << 32) | __funnelshift_r(a, b, sh);
 }
-
-#ifndef WFG_LCP64
-#define WFG_LCP64 0
+__device__ __forceinline__ int first_set(uint64_t x) { return __ffsll((long long)x) - 1; }
 #endif
 // Window of the LCP loop: 0 — 32-bit windows throughout (the default); 1 — the first window
 // 32-bit (most extensions of noisy pairs end inside it), the following ones 64-bit; 2 — 64-bit
@@ -146,7 +152,6 @@ typedef uint32_t lcpw_t;
 #endif
 
 __device__ __forceinline__ int first_set(uint32_t x) { return __ffs((int)x) - 1; }
-__device__ __forceinline__ int first_set(uint64_t x) { return __ffsll((long long)x) - 1; }
 
 // The LCP in two parts, so that the first windows of several diagonals load together:
 // lcp_first() is the XOR of the first windows (0 when nothing can match), lcp_rest()
@@ -687,7 +692,11 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   // k > hi every input read falls outside its input's [lo, hi] (the output range covers
   // them), so those lanes read nothing and store nothing.
   constexpr int U = kLeaf ? kLeafUnroll : kStepUnroll;
-  for (int kb = lo + g.tid; kb <= hi; kb += U * 32 * G) {
+  // ALIGN: ring steps start at the 32-diagonal boundary below lo, so each warp-wide access of
+  // a row covers whole 128-byte lines (lanes below lo read and write nothing).
+  constexpr bool ALIGN = !kLeaf && WFG_ALIGN_START;
+  const int k0 = ALIGN ? (lo & ~31) : lo;
+  for (int kb = k0 + g.tid; kb <= hi; kb += U * 32 * G) {
     int32_t mv[U], iv[U], dv[U];
     lcpw_t xw[U];
     #pragma unroll
@@ -696,7 +705,7 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
       iv[u] = max(mo.get(k - 1), ie.get(k - 1)) + 1;
       dv[u] = max(mo.get(k + 1), de.get(k + 1));
       int32_t m = max(dv[u], max(mx.get(k) + 1, iv[u]));
-      if (k > hi || (uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
+      if (k > hi || (ALIGN && k < lo) || (uint32_t)m > tl || (uint32_t)(m - k) > pl) m = kNull;
       mv[u] = m;
     }
     #pragma unroll
@@ -708,6 +717,7 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
     for (int u = 0; u < U; ++u) {
       const int k = kb + u * 32 * G;
       if (k > hi) break;
+      if (ALIGN && k < lo) continue;
       int32_t m = mv[u];
       if (m != kNull) {
         r[0] = min(r[0], k); r[1] = max(r[1], k);
