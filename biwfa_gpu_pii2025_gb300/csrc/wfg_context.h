@@ -56,6 +56,7 @@ struct PinBuf {
 
 constexpr int kNumPasses = 3;
 constexpr uint32_t kPlainRingCap = 4096;
+constexpr int kDirectWideSum = 32768;         // sorted schedule: plen + tlen above this takes the multi-warp launch
 constexpr int kSmemRingW = 1024;              // widest ring of the shared-memory ring shape
 constexpr int64_t kSmemRingBytes = 200 << 10;  // dynamic shared memory budget for both rings
 constexpr int kCountersPerPass = 4;  // [queue head, retry count, -, -]

@@ -530,9 +530,25 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
     for (size_t v = 1; v < cnt.size(); ++v) cnt[v] += cnt[v - 1];
     for (int i = 0; i < n; ++i)
       order[(size_t)cnt[(size_t)(c->max_sum - (c->h_plen[(size_t)i] + c->h_tlen[(size_t)i]))]++] = i;
-    Launch l; l.gw = c->force_gw; l.smem = c->force_smem; l.count = n;
-    l.batched = (sched == WFG_SCHED_PLAIN);
-    first.push_back(l);
+    // The sorted schedule sends pairs longer than kDirectWideSum (a prefix of this order)
+    // straight to a multi-warp launch with rings as wide as the batch's longest pair, on the aux
+    // stream beside the single-warp launch: a single warp would take the longest of them far
+    // beyond the rest of the batch, and their wavefronts outgrow the first pass's ring cap.
+    int n_long = 0;
+    if (sched == WFG_SCHED_SORTED && c->force_gw == 1 && !c->force_smem && c->limit_ring_w == 0)
+      while (n_long < n && c->h_plen[(size_t)order[(size_t)n_long]] + c->h_tlen[(size_t)order[(size_t)n_long]] >
+                               kDirectWideSum)
+        ++n_long;
+    if (n_long > 0) {
+      Launch lw; lw.gw = c->tune.retry_warps; lw.count = n_long; lw.order_off = 0;
+      lw.ring_w = (int)next_pow2((uint64_t)c->max_sum + 8);
+      first.push_back(lw);
+    }
+    if (n - n_long > 0 || first.empty()) {
+      Launch l; l.gw = c->force_gw; l.smem = c->force_smem; l.count = n - n_long; l.order_off = n_long;
+      l.batched = (sched == WFG_SCHED_PLAIN);
+      first.push_back(l);
+    }
   }
   if (first.empty()) { Launch l; l.count = 0; first.push_back(l); }
   // ---- shapes and arena (pass-0 launches run concurrently; retry passes reuse the arena)
@@ -578,9 +594,14 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
       return e;
     if ((e = launch_pack(n, c->d_seq.ptr, c->d_pairs.ptr, c->d_words.ptr, c->num_sms, c->stream)) != cudaSuccess) return e;
     if ((e = mark(c->ev[1])) != cudaSuccess) return e;
-    // pass 0: the first launch on the context's stream, a second one (wide pairs) on the aux
-    // stream, joined before the retry passes
+    // pass 0: the first launch on the context's stream, a second one on the aux stream,
+    // forked before the first so that the two run concurrently, joined before the retry passes
     int64_t batch_index = 0;
+    const bool fork = first.size() > 1 && first[1].count > 0 && first[0].count > 0;
+    if (fork) {
+      if ((e = cudaEventRecord(c->ev[5], c->stream)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(c->aux_stream, c->ev[5], 0)) != cudaSuccess) return e;
+    }
     for (size_t li = 0; li < first.size(); ++li) {
       const Launch& l = first[li];
       if (l.count <= 0) continue;
@@ -604,18 +625,13 @@ int wfg_run(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched) {
       kp.num_pairs_ptr = nullptr;
       kp.order = c->d_order.ptr + l.order_off;
       kp.queue_head = c->d_counters.ptr + (li == 0 ? 0 : 2);
-      cudaStream_t st = c->stream;
-      if (li > 0) {
-        if ((e = cudaEventRecord(c->ev[5], c->stream)) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(c->aux_stream, c->ev[5], 0)) != cudaSuccess) return e;
-        st = c->aux_stream;
-      }
+      const cudaStream_t st = (fork && li > 0) ? c->aux_stream : c->stream;
       if ((e = launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), st)) != cudaSuccess) return e;
       ++launches;
-      if (li > 0) {
-        if ((e = cudaEventRecord(c->ev[4], c->aux_stream)) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(c->stream, c->ev[4], 0)) != cudaSuccess) return e;
-      }
+    }
+    if (fork) {
+      if ((e = cudaEventRecord(c->ev[4], c->aux_stream)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(c->stream, c->ev[4], 0)) != cudaSuccess) return e;
     }
     if ((e = mark(c->ev[2])) != cudaSuccess) return e;
     for (int ps = 1; ps < kNumPasses; ++ps) {

@@ -281,7 +281,10 @@ typedef enum {
    * launch per bin, scratch sized from the prediction */
   WFG_SCHED_LEARNED = 1,
   WFG_SCHED_GIVEN = 2,    /* the caller's order (wfg_set_order), one persistent launch */
-  WFG_SCHED_SORTED = 3,   /* pairs sorted by length (descending), one persistent launch */
+  /* pairs sorted by length (descending), one persistent launch; pairs with plen + tlen above
+   * 32,768 take a multi-warp launch (the retry passes' shape) with rings as wide as the
+   * batch's longest pair, concurrent with the single-warp launch of the rest */
+  WFG_SCHED_SORTED = 3,
 } wfg_sched_t;
 
 typedef struct {

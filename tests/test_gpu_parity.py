@@ -120,9 +120,21 @@ def test_gpu_other_distances_through_retry_passes_and_shapes(batch_aligner, metr
 
 
 def test_gpu_long_noisy_pair_matches_oracle(batch_aligner):
-    b = pkg.PairBatch.generate(4, 2, seed=404)
+    """Two 50-100 kbp pairs at 12 % error beside short pairs: the sorted schedule sends the long
+    ones straight to the multi-warp launch with full-width rings (no retry pass), concurrently
+    with the single-warp launch of the rest."""
+    long_b = pkg.PairBatch.generate(4, 2, seed=404)
+    short = pkg.PairBatch.generate(2, 300, seed=405)
+    b = pkg.PairBatch.from_lists([long_b.pattern(i) for i in range(2)] + [short.pattern(i) for i in range(300)],
+                                 [long_b.text(i) for i in range(2)] + [short.text(i) for i in range(300)])
     res = batch_aligner.align(b)
-    for i in range(b.n):
+    assert batch_aligner.stats().retried_pairs == 0
+    _, scores, status, ops = binding.oracle_batch_time(short.seq, short.p_off, short.plen, short.t_off, short.tlen,
+                                                       threads=8, return_ops=True)
+    for j in range(300):
+        assert res.status[2 + j] == 0 and res.scores[2 + j] == scores[j]
+        assert pkg.runs_to_ops(res.runs_of(2 + j)) == ops[j]
+    for i in range(2):
         st, score, ops, _ = binding.oracle_align(b.pattern(i), b.text(i))
         assert res.status[i] == 0
         assert res.scores[i] == score
