@@ -147,6 +147,7 @@ struct wfg_context {
   cudaStream_t aux_stream = nullptr;
   // end-to-end pipeline (wfg_align_host): input copies on their own stream, per-chunk events
   cudaStream_t copy_stream = nullptr;
+  cudaStream_t alt_stream = nullptr;  // odd chunks' first passes
   int pipeline = 1;  // wfg_set_pipeline
   std::vector<cudaEvent_t> chunk_ev;
   // wfg_run's device work as a CUDA graph (wfg_set_graph)

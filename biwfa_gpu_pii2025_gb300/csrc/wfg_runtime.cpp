@@ -138,6 +138,10 @@ void wfg_context_destroy(wfg_context_t* c) {
     cudaStreamSynchronize(c->copy_stream);
     cudaStreamDestroy(c->copy_stream);
   }
+  if (c->alt_stream) {
+    cudaStreamSynchronize(c->alt_stream);
+    cudaStreamDestroy(c->alt_stream);
+  }
   for (auto& e : c->chunk_ev) cudaEventDestroy(e);
   c->d_feats.release(); c->d_pred.release(); c->d_bin_work.release(); c->h_bin_stats.release();
   c->d_batch_heads.release();
@@ -788,10 +792,12 @@ constexpr int kPipelineMaxChunks = 8;
 // End-to-end alignment with the input copy overlapped with the alignment. The pairs are cut
 // into K chunks by index. The copy stream uploads the descriptors, then the sequence bytes up
 // to each chunk's last byte, chunk by chunk. As soon as chunk k's bytes are in, the aux stream
-// packs it and (learned schedule) computes its features, predictions and binned order; the main
-// stream then runs chunk k's first pass after chunk k-1's, while later chunks are still being
-// copied. The retry passes run once, over the overflows of every chunk. Scheduling only: every
-// pair's result is the one wfg_run gives.
+// packs it and (learned schedule) computes its features, predictions and binned order; chunk
+// k's first pass then runs on the main stream (even k) or the alternate stream (odd k), in its
+// own arena region, so that it takes over the SMs as chunk k-1's persistent blocks retire —
+// a chunk's heaviest pairs take about as long as a chunk, so chunks in series would each wait
+// for their slowest pair. The retry passes run once, over the overflows of every chunk.
+// Scheduling only: every pair's result is the one wfg_run gives.
 int align_host_pipelined(wfg_context* c, const wfg_config_t* cfg, wfg_sched_t sched, int n, const char* seq,
                          int64_t seq_len, const int64_t* p_off, const int* plen, const int64_t* t_off, const int* tlen,
                          int K) {
@@ -838,19 +844,23 @@ int align_host_pipelined(wfg_context* c, const wfg_config_t* cfg, wfg_sched_t sc
     WFG_CHECK(c, c->d_bin_work.reserve((size_t)sched_bin_words()));
     WFG_CHECK(c, c->h_bin_stats.reserve((size_t)4 * K));
   }
-  // ---- arena for the first pass at the plain ring cap and for the retry passes (a chunk whose
-  // predictions need wider rings grows it between chunks)
-  const int64_t budget = arena_budget_of(c);
+  // ---- arena: two regions, for consecutive chunks' first passes that overlap (even chunks on
+  // the main stream, odd ones on the alternate stream), each sized for a first pass at the plain
+  // ring cap; the retry passes use the whole arena after both streams join. A chunk whose
+  // predictions need wider rings grows the regions between chunks.
+  const int64_t budget = arena_budget_of(c) / 2;
   Launch retry[kNumPasses];
-  int64_t arena_need = plan_retry_passes(c, p, budget, retry);
+  const int64_t retry_need = plan_retry_passes(c, p, 2 * budget, retry);
+  int64_t region = 0;
   {
     Launch l;
     l.count = cb[1] - cb[0];
     plan_first_pass(c, p, c->limit_ring_w, budget, l);
-    arena_need = std::max(arena_need, l.groups * l.L.total);
+    region = wfg_align256(l.groups * l.L.total);
   }
-  WFG_CHECK(c, c->d_arena.reserve((size_t)arena_need));
+  WFG_CHECK(c, c->d_arena.reserve((size_t)std::max(2 * region, retry_need)));
   WFG_CHECK(c, c->d_batch_heads.reserve((size_t)K));
+  if (!c->alt_stream) WFG_CHECK(c, cudaStreamCreateWithFlags(&c->alt_stream, cudaStreamNonBlocking));
   // ---- copies
   cudaStream_t cs = c->copy_stream, ms = c->stream, as = c->aux_stream;
   WFG_CHECK(c, cudaEventRecord(c->ev[6], cs));
@@ -874,7 +884,8 @@ int align_host_pipelined(wfg_context* c, const wfg_config_t* cfg, wfg_sched_t sc
   WFG_CHECK(c, cudaMemsetAsync(c->d_counters.ptr, 0, sizeof(unsigned long long) * kNumCounters, ms));
   WFG_CHECK(c, cudaMemsetAsync(c->d_batch_heads.ptr, 0, sizeof(unsigned long long) * (size_t)K, ms));
   WFG_CHECK(c, cudaEventRecord(c->ev[5], ms));
-  WFG_CHECK(c, cudaStreamWaitEvent(as, c->ev[5], 0));  // the aux stream's work follows this run's start
+  WFG_CHECK(c, cudaStreamWaitEvent(as, c->ev[5], 0));  // the aux and alternate streams follow this run's start
+  WFG_CHECK(c, cudaStreamWaitEvent(c->alt_stream, c->ev[5], 0));
   int launches = 0;
   int64_t first_warps = 0;
   int first_ring = 0;
@@ -908,20 +919,27 @@ int align_host_pipelined(wfg_context* c, const wfg_config_t* cfg, wfg_sched_t sc
       hint = (int)(c->tune.ring_margin * max_pred / p.emin) + 64;
     }
     plan_first_pass(c, p, hint, budget, l);
-    if ((size_t)(l.groups * l.L.total) > c->d_arena.cap) {
-      WFG_CHECK(c, cudaStreamSynchronize(ms));  // the earlier chunks' launches use the arena
-      WFG_CHECK(c, c->d_arena.reserve((size_t)(l.groups * l.L.total)));
+    if (l.groups * l.L.total > region) {
+      // the earlier chunks' launches use the arena: wait for them, then grow both regions
+      WFG_CHECK(c, cudaStreamSynchronize(ms));
+      WFG_CHECK(c, cudaStreamSynchronize(c->alt_stream));
+      region = wfg_align256(l.groups * l.L.total);
+      WFG_CHECK(c, c->d_arena.reserve((size_t)std::max(2 * region, retry_need)));
     }
-    WFG_CHECK(c, cudaStreamWaitEvent(ms, ready, 0));
+    l.arena_off = (k & 1) * region;
+    const cudaStream_t ks = (k & 1) ? c->alt_stream : ms;
+    WFG_CHECK(c, cudaStreamWaitEvent(ks, ready, 0));
     KernelParams kp = launch_params(c, cfg, p, l, 0);
     kp.num_pairs = m;
     kp.num_pairs_ptr = nullptr;
     kp.order = c->d_order.ptr + a;
     kp.queue_head = c->d_batch_heads.ptr + k;
-    WFG_CHECK(c, launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), ms));
+    WFG_CHECK(c, launch_biwfa(kp, (int)(l.groups / biwfa_groups_per_block(l.gw, l.smem)), ks));
     ++launches;
     if (k == 0) { first_warps = l.groups * l.gw; first_ring = l.ring_w; first_arena = l.L.total; }
   }
+  WFG_CHECK(c, cudaEventRecord(c->ev[4], c->alt_stream));
+  WFG_CHECK(c, cudaStreamWaitEvent(ms, c->ev[4], 0));
   WFG_CHECK(c, cudaEventRecord(c->ev[2], ms));
   for (int ps = 1; ps < kNumPasses; ++ps) {
     const Launch& l = retry[ps];
