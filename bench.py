@@ -237,16 +237,26 @@ def cpu_baseline(batch, workload: int = 5, threads: int | None = None, metric: i
     return out
 
 
-def parity_check(batch, res, penalties=PENALTIES, metric: int = 0) -> dict:
-    """Every pair of the timed batch against the oracle (status, score and the whole operation
-    string), on all host threads, outside the timed region."""
+# Pairs of the timed batch checked bit-exactly by the parity leg: every pair, except on the long
+# noisy workload (a seeded sample; each of its pairs takes seconds of CPU).
+PARITY_SAMPLE = {4: 256}
+
+
+def parity_check(batch, res, workload: int = 5, penalties=PENALTIES, metric: int = 0) -> dict:
+    """The timed batch against WFA2-lib itself where it is built here, else the oracle (status,
+    score and the whole operation string of each pair), on all host threads, outside the timed
+    region."""
     from oracle import binding
     against = "wfa2" if metric == 0 and binding.ref_lib() is not None else "oracle"
+    idx, which = None, "every pair of the timed batch"
+    if workload in PARITY_SAMPLE and batch.n > PARITY_SAMPLE[workload]:
+        idx = np.sort(np.random.default_rng(7).choice(batch.n, PARITY_SAMPLE[workload], replace=False))
+        which = f"{PARITY_SAMPLE[workload]} pairs of the timed batch (seeded sample)"
     r = binding.check_batch(batch.seq, batch.p_off, batch.plen, batch.t_off, batch.tlen, res.scores, res.status,
-                            res.runs, res.run_off, res.run_len, penalties, metric=metric, against=against)
+                            res.runs, res.run_off, res.run_len, penalties, metric=metric, against=against, idx=idx)
     return {"checked": r["checked"], "mismatches": r["mismatches"], "first_bad": r["first_bad"],
-            "against": ("WFA2-lib v2.3 itself (ultralow BiWFA), every pair of the timed batch" if against == "wfa2"
-                        else "the oracle (C restatement of WFA2-lib v2.3 BiWFA), every pair of the timed batch")}
+            "against": ("WFA2-lib v2.3 itself (ultralow BiWFA), " if against == "wfa2"
+                        else "the oracle (C restatement of WFA2-lib v2.3 BiWFA), ") + which}
 
 
 def run_reference(args):
@@ -342,7 +352,7 @@ def run_ours(args):
     name, n_full = WORKLOADS[wl]
     n = args.pairs or n_full
     al = pkg.BatchAligner(local if world > 1 else 0)
-    learned = not args.plain_only
+    learned = not args.plain_only and args.sched == "learned"
     pred, learn_info = None, None
     if learned:
         pred, learn_info = train_predictor(pkg, al, wl, min(200_000, max(n, 2000)), rank)
@@ -356,10 +366,17 @@ def run_ours(args):
     plain_ms, plain_kernel_ms, _, _, _ = time_path(al, _capi.SCHED_PLAIN, args.steps, args.warmup, dist)
     plain_res = al.fetch()
     sorted_ms, _, _, _, _ = time_path(al, _capi.SCHED_SORTED, args.steps, args.warmup, dist)
-    sched = _capi.SCHED_LEARNED if learned else _capi.SCHED_PLAIN
-    sched_name = ("learned-binned persistent (MLP score prediction orders and bins pairs, sizes scratch; "
-                  "autotuned warps-per-pair and shared-memory rings)"
-                  if learned else "plain length-sorted batched launches")
+    if learned:
+        sched = _capi.SCHED_LEARNED
+        sched_name = ("learned-binned persistent (MLP score prediction orders and bins pairs, sizes scratch; "
+                      "autotuned warps-per-pair and shared-memory rings)")
+    elif args.sched == "sorted" and not args.plain_only:
+        sched = _capi.SCHED_SORTED
+        sched_name = ("length-sorted persistent (pairs above 32,768 bp total on 8-warp groups with full-width "
+                      "rings, concurrently)")
+    else:
+        sched = _capi.SCHED_PLAIN
+        sched_name = "plain length-sorted batched launches"
     step_ms, kernel_ms, launches, clk, retried = time_path(al, sched, args.steps, args.warmup, dist,
                                                            ClockSampler(local if world > 1 else 0))
     res = al.fetch()
@@ -447,7 +464,7 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(batch, wl)
         # the oracle as the checker (untimed): every pair of this step's batch, bit-exact
-        line["parity"] = parity_check(batch, res)
+        line["parity"] = parity_check(batch, res, wl)
     al.close()
     dist.close()
     if rank == 0:
@@ -558,6 +575,8 @@ def main():
     ap.add_argument("--pairs", type=int, default=0, help="override the workload's pair count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time only the plain length-sorted path")
+    ap.add_argument("--sched", choices=["learned", "sorted", "plain"], default="learned",
+                    help="the schedule whose throughput is `value` (learned: trains the predictor first)")
     ap.add_argument("--distances", action="store_true",
                     help="one line per distance (gap-affine, two-piece, gap-linear, edit, indel)")
     ap.add_argument("--only", default="", help="with --distances: the distances whose name contains this text")
