@@ -31,13 +31,19 @@ constexpr int kAbsent = INT32_MAX;         // lo of a wavefront that does not ex
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxScope = WFG_MAX_SCOPE;       // score scope cap of the usual kernels (32)
 constexpr int kMaxScope2p = WFG_MAX_SCOPE_2P;  // the cap of the large-scope and two-piece kernels (64)
+#ifndef WFG_G1_GROUPS
+#define WFG_G1_GROUPS 4
+#endif
 #ifndef WFG_G1_MIN_BLOCKS
-#define WFG_G1_MIN_BLOCKS 7
+#define WFG_G1_MIN_BLOCKS (28 / WFG_G1_GROUPS)
 #endif
 #ifndef WFG_STEP_UNROLL
 #define WFG_STEP_UNROLL 2
 #endif
-constexpr int kMinBlocksPerSM = WFG_G1_MIN_BLOCKS;  // 7: caps registers at 72 so 28 warps fit on an SM
+// Single-warp shape: kG1Groups pairs (warps) per block, kMinBlocksPerSM blocks per SM — 28 warps,
+// which caps registers at 72.
+constexpr int kG1Groups = WFG_G1_GROUPS;
+constexpr int kMinBlocksPerSM = WFG_G1_MIN_BLOCKS;
 #ifndef WFG_LEAF_UNROLL
 #define WFG_LEAF_UNROLL 2
 #endif
@@ -1429,7 +1435,7 @@ namespace {
 // instantiations: three components with a score scope up to 32 (the usual penalties), three
 // components up to 64, and five components (two-piece gap-affine) up to 64.
 // Dynamic shared memory of the single-warp shape: the groups' packed-sequence slots.
-constexpr size_t kSeqSmemBytesG1 = (size_t)4 * kSeqSmemWords * sizeof(uint32_t);
+constexpr size_t kSeqSmemBytesG1 = (size_t)kG1Groups * kSeqSmemWords * sizeof(uint32_t);
 
 template <int G, int GROUPS, bool RS, int MINB, bool TWO, int MS>
 cudaError_t launch_shape(const KernelParams& p, int grid, cudaStream_t stream) {
@@ -1459,7 +1465,7 @@ cudaError_t occupancy_of(size_t dyn, int* blocks_per_sm) {
 
 template <bool TWO, int MS>
 cudaError_t occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm) {
-  if (gw <= 1) return occupancy_of<1, 4, false, kMinBlocksPerSM, TWO, MS>(kSeqSmemBytesG1, blocks_per_sm);
+  if (gw <= 1) return occupancy_of<1, kG1Groups, false, kMinBlocksPerSM, TWO, MS>(kSeqSmemBytesG1, blocks_per_sm);
   if (gw == 8) {
     if (ring_in_smem) return occupancy_of<8, 1, true, 1, TWO, MS>(dyn, blocks_per_sm);
     return occupancy_of<8, 1, false, 2, TWO, MS>(0, blocks_per_sm);
@@ -1471,7 +1477,7 @@ cudaError_t occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_pe
 template <bool TWO, int MS>
 cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) {
   const int gw = p.group_warps > 0 ? p.group_warps : 1;
-  if (gw == 1) return launch_shape<1, 4, false, kMinBlocksPerSM, TWO, MS>(p, grid, stream);
+  if (gw == 1) return launch_shape<1, kG1Groups, false, kMinBlocksPerSM, TWO, MS>(p, grid, stream);
   if (gw == 8) {
     if (p.ring_in_smem) return launch_shape<8, 1, true, 1, TWO, MS>(p, grid, stream);
     return launch_shape<8, 1, false, 2, TWO, MS>(p, grid, stream);
@@ -1485,10 +1491,10 @@ cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) 
 
 }  // namespace
 
-int biwfa_warps_per_block() { return 4; }
+int biwfa_warps_per_block() { return kG1Groups; }
 
 cudaError_t biwfa_occupancy(int* blocks_per_sm) {
-  return occupancy_of<1, 4, false, kMinBlocksPerSM, false, kMaxScope>(kSeqSmemBytesG1, blocks_per_sm);
+  return occupancy_of<1, kG1Groups, false, kMinBlocksPerSM, false, kMaxScope>(kSeqSmemBytesG1, blocks_per_sm);
 }
 
 // The kernel instantiation of a launch: 0 three components (scope <= 32), 1 three components
@@ -1508,7 +1514,7 @@ cudaError_t biwfa_occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blo
 // Groups (pairs in flight) per block of a shape.
 int biwfa_groups_per_block(int group_warps, int ring_in_smem) {
   (void)ring_in_smem;
-  return group_warps <= 1 ? 4 : 1;
+  return group_warps <= 1 ? kG1Groups : 1;
 }
 
 cudaError_t launch_biwfa(const KernelParams& p, int grid, cudaStream_t stream) {
