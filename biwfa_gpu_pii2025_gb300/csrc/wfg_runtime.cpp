@@ -786,18 +786,21 @@ int wfg_fetch(wfg_context_t* c, int* scores, int* statuses, int64_t* run_off, in
 namespace {
 
 constexpr int kPipelineMinPairs = 131072;  // batches from which wfg_align_host overlaps its input copy
-constexpr int kPipelinePairsPerChunk = 65536;
-constexpr int kPipelineMaxChunks = 8;
+constexpr int kPipelineHeadDiv = 8;        // the head chunk: the first 1/8 of the pairs
 
 // End-to-end alignment with the input copy overlapped with the alignment. The pairs are cut
-// into K chunks by index. The copy stream uploads the descriptors, then the sequence bytes up
-// to each chunk's last byte, chunk by chunk. As soon as chunk k's bytes are in, the aux stream
+// into chunks by index: a head of 1/8 of the pairs, then the rest (K = 2; the code takes any
+// K, the head fixed). The copy stream uploads the descriptors, then the sequence bytes up to
+// each chunk's last byte, chunk by chunk. As soon as chunk k's bytes are in, the aux stream
 // packs it and (learned schedule) computes its features, predictions and binned order; chunk
 // k's first pass then runs on the main stream (even k) or the alternate stream (odd k), in its
-// own arena region, so that it takes over the SMs as chunk k-1's persistent blocks retire —
-// a chunk's heaviest pairs take about as long as a chunk, so chunks in series would each wait
-// for their slowest pair. The retry passes run once, over the overflows of every chunk.
-// Scheduling only: every pair's result is the one wfg_run gives.
+// own arena region, so that it takes over the SMs as chunk k-1's persistent warps retire. The
+// head's alignment outlasts the copy of everything else, and the rest then runs in one
+// launch, heaviest first: with many equal chunks, each chunk's heaviest pairs (about 0.3 s for
+// one warp) started only when the chunk did, and the last chunk's ones ended after the rest
+// (measured: 8 equal chunks cost 190 ms of device time, as much as the copy they hid). The
+// retry passes run once, over the overflows of every chunk. Scheduling only: every pair's
+// result is the one wfg_run gives.
 int align_host_pipelined(wfg_context* c, const wfg_config_t* cfg, wfg_sched_t sched, int n, const char* seq,
                          int64_t seq_len, const int64_t* p_off, const int* plen, const int64_t* t_off, const int* tlen,
                          int K) {
@@ -817,9 +820,10 @@ int align_host_pipelined(wfg_context* c, const wfg_config_t* cfg, wfg_sched_t sc
   std::vector<int> cb((size_t)K + 1);
   std::vector<int64_t> hi((size_t)K);
   int64_t end = 0;
+  const int head = n / kPipelineHeadDiv;
   for (int k = 0; k < K; ++k) {
-    cb[(size_t)k] = (int)((int64_t)n * k / K);
-    cb[(size_t)k + 1] = (int)((int64_t)n * (k + 1) / K);
+    cb[(size_t)k] = k == 0 ? 0 : head + (int)((int64_t)(n - head) * (k - 1) / (K - 1));
+    cb[(size_t)k + 1] = head + (int)((int64_t)(n - head) * k / (K - 1));
     for (int i = cb[(size_t)k]; i < cb[(size_t)k + 1]; ++i)
       end = std::max(end, std::max(p_off[i] + plen[i], t_off[i] + tlen[i]));
     hi[(size_t)k] = end;
@@ -982,7 +986,7 @@ int wfg_align_host(wfg_context_t* c, const wfg_config_t* cfg, wfg_sched_t sched,
                          (sched == WFG_SCHED_SORTED || (sched == WFG_SCHED_LEARNED && c->model != nullptr &&
                                                         single_warp_policy));
   if (pipelined) {
-    const int K = std::min(kPipelineMaxChunks, std::max(2, n / kPipelinePairsPerChunk));
+    const int K = 2;
     const int st = align_host_pipelined(c, cfg, sched, n, seq, seq_len, p_off, plen, t_off, tlen, K);
     if (st != WF_STATUS_ALG_COMPLETED) return st;
     return wfg_fetch(c, scores, statuses, run_off, run_len, runs, runs_cap, total_runs);

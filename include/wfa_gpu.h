@@ -329,11 +329,11 @@ int wfg_fetch(wfg_context_t* ctx, int* scores, int* statuses, int64_t* run_off, 
               uint32_t* runs, int64_t runs_cap, int64_t* total_runs);
 /* Upload + run + fetch in one call (the end-to-end path). Batches of 131,072 pairs or more on
  * WFG_SCHED_SORTED, or on WFG_SCHED_LEARNED with an attached model and a single-warp policy,
- * overlap the input copy with the alignment: the pairs are cut into up to 8 chunks by index,
- * and each chunk is packed, predicted, ordered and run (first pass) as soon as its bytes are
- * on the device, while later chunks are still being copied; the retry passes run once at the
- * end. This pays when the pairs' bytes lie in the buffer in pair order. Results are the same
- * as upload + run + fetch. */
+ * overlap the input copy with the alignment: the first 1/8 of the pairs (by index) is packed,
+ * predicted, ordered and run (first pass) as soon as its bytes are on the device, while the
+ * rest is still being copied; the rest then runs as one launch as the head's warps retire, and
+ * the retry passes once at the end. This pays when the pairs' bytes lie in the buffer in pair
+ * order. Results are the same as upload + run + fetch. */
 int wfg_align_host(wfg_context_t* ctx, const wfg_config_t* cfg, wfg_sched_t sched,
                    int num_pairs, const char* seq, int64_t seq_len,
                    const int64_t* p_off, const int* plen, const int64_t* t_off, const int* tlen,
