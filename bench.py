@@ -399,11 +399,14 @@ def run_ours(args):
     achieved = alg_bytes / (k_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     counters = profile_counters()
+    if counters and counters.get("workload_id") != wl:
+        counters = None  # captured on another workload
     traffic = None
-    if counters and counters.get("pairs"):
-        # the capture's DRAM bytes per pair of its launch, times this launch's pairs (the same
-        # workload generator; the capture is one full launch when its pairs equal n)
-        traffic = float(counters["dram_bytes_read"] + counters["dram_bytes_write"]) / counters["pairs"] * n
+    if counters:
+        # DRAM bytes of one whole first-pass launch over the bench's pairs (ncu, one pass), per
+        # pair, times this launch's pairs
+        full = counters.get("full_launch") or counters
+        traffic = float(full["dram_bytes_read"] + full["dram_bytes_write"]) / full["pairs"] * n
 
     # ---- end to end through the public API with pinned host buffers
     pin = pkg.PinnedHost()
