@@ -7,7 +7,11 @@
 A step aligns the whole synthetic batch once (pack + BiWFA on the device), inputs resident
 in HBM, L2 flushed before every step (512 MiB write). The default workload is the 1,000,000-
 pair equal mixture of the 1 kbp / 5 %, 150 bp / 2 % and uneven 100 bp-10 kbp / 1-10 %
-workloads (seeded). Prints one JSON line.
+workloads (seeded). Prints one JSON line; besides `value` it carries the plain batched and sorted
+persistent schedules, `e2e` (the same batch through wfg_align_host from pinned host memory, the
+input copy overlapped with the alignment), the roofline with the kernel's ncu counters, the CPU
+baseline and `parity` (every pair of the timed batch checked bit-exactly, outside the timing).
+`--sched sorted` values the sorted persistent schedule instead of the learned one (no training).
 
 --impl reference times the reference's own CPU algorithm on this machine's host cores: WFA2-lib's
 BiWFA itself, compiled on this machine from the unmodified copy of its sources in the git-ignored
