@@ -34,18 +34,27 @@ constexpr int kMaxScope2p = WFG_MAX_SCOPE_2P;  // the cap of the large-scope and
 #ifndef WFG_G1_GROUPS
 #define WFG_G1_GROUPS 1
 #endif
-#ifndef WFG_G1_MIN_BLOCKS
-#define WFG_G1_MIN_BLOCKS (28 / WFG_G1_GROUPS)
+#ifndef WFG_G1_WARPS3
+#define WFG_G1_WARPS3 32
+#endif
+#ifndef WFG_G1_WARPS5
+#define WFG_G1_WARPS5 28
 #endif
 #ifndef WFG_STEP_UNROLL
 #define WFG_STEP_UNROLL 2
 #endif
-// Single-warp shape: kG1Groups pairs (warps) per block, kMinBlocksPerSM blocks per SM — 28 warps,
-// which caps registers at 72. One warp per block (measured equal to four on the 1M-pair mixture:
-// 2,457 vs 2,459 ms) lets each warp retire on its own when its queue drains, so a launch that
-// follows on another stream takes over warp slots at once instead of waiting for whole blocks.
+// Single-warp shape: kG1Groups pairs (warps) per block; resident warps per SM fix the register
+// cap. The three-component kernels keep 32 warps per SM (64 registers), the two-piece one 28
+// (72 registers). Measured (same GB300, identical results) against 28 warps for all: gap-affine
+// mixture 1.3 % faster, uneven pairs 1.6 %, edit mixture 5.4 % faster, 150 bp pairs 2.6 %
+// slower, two-piece mixture 7.9 % slower (its step spills at 64 registers); 36 warps (56
+// registers) 4 % and 40 warps (48 registers) 15 % slower on the gap-affine mixture. One warp
+// per block (measured equal to four: 2,457 vs 2,459 ms) lets each warp retire on its own when
+// its queue drains, so a launch that follows on another stream takes over warp slots at once
+// instead of waiting for whole blocks.
 constexpr int kG1Groups = WFG_G1_GROUPS;
-constexpr int kMinBlocksPerSM = WFG_G1_MIN_BLOCKS;
+template <bool TWO>
+constexpr int g1_min_blocks() { return (TWO ? WFG_G1_WARPS5 : WFG_G1_WARPS3) / kG1Groups; }
 #ifndef WFG_LEAF_UNROLL
 #define WFG_LEAF_UNROLL 2
 #endif
@@ -1497,7 +1506,7 @@ cudaError_t occupancy_of(size_t dyn, int* blocks_per_sm) {
 
 template <bool TWO, int MS>
 cudaError_t occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_per_sm) {
-  if (gw <= 1) return occupancy_of<1, kG1Groups, false, kMinBlocksPerSM, TWO, MS>(kSeqSmemBytesG1, blocks_per_sm);
+  if (gw <= 1) return occupancy_of<1, kG1Groups, false, g1_min_blocks<TWO>(), TWO, MS>(kSeqSmemBytesG1, blocks_per_sm);
   if (gw == 8) {
     if (ring_in_smem) return occupancy_of<8, 1, true, 1, TWO, MS>(dyn, blocks_per_sm);
     return occupancy_of<8, 1, false, 2, TWO, MS>(0, blocks_per_sm);
@@ -1509,7 +1518,7 @@ cudaError_t occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_pe
 template <bool TWO, int MS>
 cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) {
   const int gw = p.group_warps > 0 ? p.group_warps : 1;
-  if (gw == 1) return launch_shape<1, kG1Groups, false, kMinBlocksPerSM, TWO, MS>(p, grid, stream);
+  if (gw == 1) return launch_shape<1, kG1Groups, false, g1_min_blocks<TWO>(), TWO, MS>(p, grid, stream);
   if (gw == 8) {
     if (p.ring_in_smem) return launch_shape<8, 1, true, 1, TWO, MS>(p, grid, stream);
     return launch_shape<8, 1, false, 2, TWO, MS>(p, grid, stream);
@@ -1526,7 +1535,7 @@ cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) 
 int biwfa_warps_per_block() { return kG1Groups; }
 
 cudaError_t biwfa_occupancy(int* blocks_per_sm) {
-  return occupancy_of<1, kG1Groups, false, kMinBlocksPerSM, false, kMaxScope>(kSeqSmemBytesG1, blocks_per_sm);
+  return occupancy_of<1, kG1Groups, false, g1_min_blocks<false>(), false, kMaxScope>(kSeqSmemBytesG1, blocks_per_sm);
 }
 
 // The kernel instantiation of a launch: 0 three components (scope <= 32), 1 three components
