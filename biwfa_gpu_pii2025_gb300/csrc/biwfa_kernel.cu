@@ -56,10 +56,15 @@ constexpr int kG1Groups = WFG_G1_GROUPS;
 template <bool TWO>
 constexpr int g1_min_blocks() { return (TWO ? WFG_G1_WARPS5 : WFG_G1_WARPS3) / kG1Groups; }
 #ifndef WFG_LEAF_UNROLL
-#define WFG_LEAF_UNROLL 2
+#define WFG_LEAF_UNROLL 1
 #endif
 constexpr int kStepUnroll = WFG_STEP_UNROLL;        // diagonals per thread per step iteration (rings)
-constexpr int kLeafUnroll = WFG_LEAF_UNROLL;        // the same for the leaf store (narrower steps)
+// The same for the leaf store (narrower steps). One diagonal per thread there, measured against
+// two at 32 warps per SM (same GB300, identical results): gap-affine mixture 3.2 % faster,
+// 1 kbp pairs 6.7 %, 150 bp pairs 4.3 %, uneven pairs 2.4 %, two-piece equal, edit 2.8 %
+// slower; three diagonals 3.5 % slower on the mixture. In the ring steps two per thread stay
+// best (one 4.3 %, three 8.7 % slower).
+constexpr int kLeafUnroll = WFG_LEAF_UNROLL;
 constexpr int ST_OK = -1, ST_END_REACHED = -2, ST_END_UNREACHABLE = -3;
 constexpr int CM = 0, CI = 1, CI2 = 2, CD = 3, CD2 = 4;  // components (affine2p_matrix_type values)
 constexpr int kFallbackMinScore = 250, kFallbackMinLength = 100, kRecoveryMinScore = 500;
