@@ -63,7 +63,8 @@ constexpr int kStepUnroll = WFG_STEP_UNROLL;        // diagonals per thread per 
 // two at 32 warps per SM (same GB300, identical results): gap-affine mixture 3.2 % faster,
 // 1 kbp pairs 6.7 %, 150 bp pairs 4.3 %, uneven pairs 2.4 %, two-piece equal, edit 2.8 %
 // slower; three diagonals 3.5 % slower on the mixture. In the ring steps two per thread stay
-// best (one 4.3 %, three 8.7 % slower).
+// best (one 4.3 %, three 8.7 % slower). The multi-warp shapes keep two in the leaf steps (the
+// 50-100 kbp pairs on 8-warp groups: 28.8 s with two, 30.5 s with one).
 constexpr int kLeafUnroll = WFG_LEAF_UNROLL;
 constexpr int ST_OK = -1, ST_END_REACHED = -2, ST_END_UNREACHABLE = -3;
 constexpr int CM = 0, CI = 1, CI2 = 2, CD = 3, CD2 = 4;  // components (affine2p_matrix_type values)
@@ -742,7 +743,7 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   // U diagonals per thread per iteration, so that their loads are in flight together. For
   // k > hi every input read falls outside its input's [lo, hi] (the output range covers
   // them), so those lanes read nothing and store nothing.
-  constexpr int U = kLeaf ? kLeafUnroll : kStepUnroll;
+  constexpr int U = kLeaf ? (G == 1 ? kLeafUnroll : 2) : kStepUnroll;
   // ALIGN: ring steps start at the 32-diagonal boundary below lo, so each warp-wide access of
   // a row covers whole 128-byte lines (lanes below lo read and write nothing).
   constexpr bool ALIGN = !kLeaf && WFG_ALIGN_START;
