@@ -82,10 +82,8 @@ __device__ __forceinline__ int comp_index(int c) {
 #ifndef WFG_RING16
 #define WFG_RING16 0
 #endif
-// Element type of the modular rings (the breakpoint search's wavefronts): int32 (the default),
-// or int16 when WFG_RING16 — valid only while every offset of a batch stays below 32,767.
-// Measured on the 1M-pair mixture (same GB300, identical results): int16 rings 10 % slower —
-// the kernel waits on load latency, not on DRAM bytes, and the conversions add instructions.
+// Element type of the modular rings (the breakpoint search's wavefronts): int32, or int16 when
+// WFG_RING16 — valid only while every offset of a batch stays below 32,767.
 #if WFG_RING16
 typedef int16_t ring_t;
 #else
