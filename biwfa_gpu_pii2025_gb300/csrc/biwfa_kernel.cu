@@ -79,52 +79,23 @@ __device__ __forceinline__ int comp_index(int c) {
   return c == CM ? 0 : c == CI ? 1 : c == CD ? 2 : c == CI2 ? 3 : 4;
 }
 
-#ifndef WFG_RING16
-#define WFG_RING16 0
-#endif
-// Element type of the modular rings (the breakpoint search's wavefronts): int32, or int16 when
-// WFG_RING16 — valid only while every offset of a batch stays below 32,767.
-#if WFG_RING16
-typedef int16_t ring_t;
-#else
-typedef int32_t ring_t;
-#endif
-
-// Stored element <-> offset. An int16 ring keeps a null (or any negative, null-derived value)
-// as INT16_MIN.
-__device__ __forceinline__ int32_t widen(int32_t v) { return v; }
-template <typename T> __device__ __forceinline__ T narrow(int32_t v);
-template <> __device__ __forceinline__ int32_t narrow<int32_t>(int32_t v) { return v; }
-#if WFG_RING16
-__device__ __forceinline__ int32_t widen(int16_t v) { return v == INT16_MIN ? kNull : (int32_t)v; }
-template <> __device__ __forceinline__ int16_t narrow<int16_t>(int32_t v) { return v < 0 ? (int16_t)INT16_MIN : (int16_t)v; }
-#endif
-
 // A view of one stored wavefront. Offsets for diagonal k live at base[(k - kbase) & mask]:
 // rings use kbase = 0 and a power-of-two mask (circular over diagonals), the leaf store
 // uses kbase = the allocation's first diagonal and mask = ~0.
-template <typename T>
-struct WfRefT {
+struct WfRef {
   int lo, hi;
-  T* base;
+  int32_t* base;
   int kbase;
   uint32_t mask;
   __device__ __forceinline__ bool present() const { return lo != kAbsent; }
   __device__ __forceinline__ bool nonnull() const { return lo <= hi; }
-  __device__ __forceinline__ int32_t at(int k) const { return widen(base[(uint32_t)(k - kbase) & mask]); }
-  __device__ __forceinline__ void put(int k, int32_t v) const { base[(uint32_t)(k - kbase) & mask] = narrow<T>(v); }
+  __device__ __forceinline__ int32_t at(int k) const { return base[(uint32_t)(k - kbase) & mask]; }
+  __device__ __forceinline__ void put(int k, int32_t v) const { base[(uint32_t)(k - kbase) & mask] = v; }
   __device__ __forceinline__ int32_t get(int k) const { return (k >= lo && k <= hi) ? at(k) : kNull; }
 };
-typedef WfRefT<int32_t> WfRef;     // the leaf store
-typedef WfRefT<ring_t> RingRef;    // the rings
-// The reference type of a storage mode (0 ring, 1 leaf store).
-template <int MODE> struct RefOfT { typedef RingRef type; };
-template <> struct RefOfT<1> { typedef WfRef type; };
-template <int MODE> using RefOf = typename RefOfT<MODE>::type;
 
-template <typename R = WfRef>
-__device__ __forceinline__ R absent_ref() {
-  R r;
+__device__ __forceinline__ WfRef absent_ref() {
+  WfRef r;
   r.lo = kAbsent; r.hi = INT_MIN; r.base = nullptr; r.kbase = 0; r.mask = 0;
   return r;
 }
@@ -300,7 +271,7 @@ struct DirCfg {
   int2* rdesc;       // ring descriptors [scope*3] (shared memory)
   int2* rdesc2;      // I2/D2 ring descriptors [scope*2] (warp arena; nc == 5 only)
   int* rphys;        // physical buffer of each ring slot [scope] (shared memory)
-  ring_t* rdata;     // ring storage [nphys*3][W], then I2/D2 [nphys*2][W] when nc == 5
+  int32_t* rdata;    // ring storage [nphys*3][W], then I2/D2 [nphys*2][W] when nc == 5
   int4* ldesc;       // leaf descriptors [(lmax+1)*3] {lo, hi, data_off, kbase}, then I2/D2 [(lmax+1)*2]
   int32_t* ldata;
 };
@@ -321,12 +292,14 @@ __device__ __forceinline__ int slot_of(const DirCfg& c, int score) {
   return score - c.scope * (int)__umulhi((uint32_t)score, c.magic);
 }
 
-// MODE: 0 ring, 1 leaf store. An absent ring reference keeps the ring's base, kbase and mask
-// (never dereferenced: its range is empty), so that every ring reference of a step shares them.
-template <int MODE>
-__device__ __forceinline__ RefOf<MODE> ref_raw(const DirCfg& c, int score, int ci) {
-  RefOf<MODE> r;
-  if constexpr (MODE == 0) {
+// MODE: 0 ring, 1 leaf store, -1 read from the configuration (callers that serve both).
+// An absent ring reference keeps the ring's base, kbase and mask (never dereferenced: its
+// range is empty), so that every ring reference of a step shares them.
+template <int MODE = -1>
+__device__ __forceinline__ WfRef ref_raw(const DirCfg& c, int score, int ci) {
+  WfRef r;
+  const bool leaf = MODE < 0 ? (c.leaf != 0) : (MODE == 1);
+  if (!leaf) {
     r.kbase = 0; r.mask = (uint32_t)c.W - 1u;
     if (score < 0) { r.lo = kAbsent; r.hi = INT_MIN; r.base = c.rdata; return r; }
     const int slot = slot_of(c, score);
@@ -335,7 +308,7 @@ __device__ __forceinline__ RefOf<MODE> ref_raw(const DirCfg& c, int score, int c
     const int buf = ci < 3 ? c.rphys[slot] * 3 + ci : c.nphys * 3 + c.rphys[slot] * 2 + (ci - 3);
     r.base = c.rdata + (size_t)buf * (size_t)c.W;
   } else {
-    if (score < 0 || score > c.lmax) return absent_ref<WfRef>();
+    if (score < 0 || score > c.lmax) return absent_ref();
     const int4 ds = ci < 3 ? c.ldesc[score * 3 + ci] : c.ldesc[(c.lmax + 1) * 3 + score * 2 + (ci - 3)];
     r.lo = ds.x; r.hi = ds.y;
     r.base = c.ldata + ds.z;
@@ -345,9 +318,9 @@ __device__ __forceinline__ RefOf<MODE> ref_raw(const DirCfg& c, int score, int c
 }
 // Input fetch: absent when the score is negative, the slot is empty or the wavefront is
 // null (wavefront_compute_get_*wavefront).
-template <int MODE>
-__device__ __forceinline__ RefOf<MODE> fetch(const DirCfg& c, int score, int ci) {
-  RefOf<MODE> r = ref_raw<MODE>(c, score, ci);
+template <int MODE = -1>
+__device__ __forceinline__ WfRef fetch(const DirCfg& c, int score, int ci) {
+  WfRef r = ref_raw<MODE>(c, score, ci);
   if (!r.nonnull()) { r.lo = kAbsent; r.hi = INT_MIN; }
   return r;
 }
@@ -411,11 +384,11 @@ __device__ void dir_init(Dir& d, const SeqView& sv, int cb, int ce) {
 
 // wavefront_extend_end2end(_max) + wavefront_termination_end2end. Returns 1 when the
 // direction is finished (end reached or unreachable).
-template <int G, int MODE>
+template <int G>
 __device__ __noinline__ int dir_extend(Dir& d, int s, const Grp<G> g, int* max_ak_out) {
   const DirCfg c = d.cfg;
   if (max_ak_out) *max_ak_out = 0;
-  const RefOf<MODE> m = ref_raw<MODE>(c, s, 0);
+  const WfRef m = ref_raw(c, s, 0);
   if (!m.present()) {
     if (d.num_null > c.scope) { d.status = ST_END_UNREACHABLE; d.status_score = s; return 1; }
     return 0;
@@ -434,7 +407,7 @@ __device__ __noinline__ int dir_extend(Dir& d, int s, const Grp<G> g, int* max_a
   g.minmax(my, mx1);
   g.sync();
   const int ak = sv.tlen - sv.plen;
-  const RefOf<MODE> t = (ce == CM) ? m : ref_raw<MODE>(c, s, comp_index(ce));
+  const WfRef t = (ce == CM) ? m : ref_raw(c, s, comp_index(ce));
   const bool done = (t.lo <= ak && ak <= t.hi) && (t.at(ak) >= sv.tlen);
   if (done) { d.status = ST_END_REACHED; d.status_score = s; d.end_k = ak; return 1; }
   if (max_ak_out) *max_ak_out = my[0];
@@ -463,12 +436,12 @@ __device__ __noinline__ int dir_step_linear(Dir& d, const Pen p, int s, const Gr
   const bool edit = p.metric == kMetricEdit;
   *max_ak_out = 0;
   if (kLeaf && s > c.lmax) return -1;
-  const RefOf<MODE> pv = ref_raw<MODE>(c, s - 1, 0);  // the previous M wavefront (possibly null)
+  const WfRef pv = ref_raw<MODE>(c, s - 1, 0);  // the previous M wavefront (possibly null)
   const int lo = pv.lo - 1, hi = pv.hi + 1;
   const int width = hi - lo + 1;
-  RefOf<MODE> om, os;  // output M, pre-extension scratch
+  WfRef om, os;  // output M, pre-extension scratch
   int offm = 0, need = 0;
-  if constexpr (!kLeaf) {
+  if (!kLeaf) {
     if (width > c.W) return -1;
     om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
     os.base = om.base + c.W;
@@ -562,13 +535,13 @@ __device__ __noinline__ int dir_step_2p(Dir& d, const Pen p, int s, const Grp<G>
   const uint32_t tl = (uint32_t)sv.tlen, pl = (uint32_t)sv.plen;
   *max_ak_out = 0;
   if (kLeaf && s > c.lmax) return -1;
-  const RefOf<MODE> mx = fetch<MODE>(c, s - p.x, 0);
-  const RefOf<MODE> mo1 = fetch<MODE>(c, s - p.o - p.e, 0);
-  const RefOf<MODE> ie1 = fetch<MODE>(c, s - p.e, 1);
-  const RefOf<MODE> de1 = fetch<MODE>(c, s - p.e, 2);
-  const RefOf<MODE> mo2 = fetch<MODE>(c, s - c.o2 - c.e2, 0);
-  const RefOf<MODE> ie2 = fetch<MODE>(c, s - c.e2, 3);
-  const RefOf<MODE> de2 = fetch<MODE>(c, s - c.e2, 4);
+  const WfRef mx = fetch<MODE>(c, s - p.x, 0);
+  const WfRef mo1 = fetch<MODE>(c, s - p.o - p.e, 0);
+  const WfRef ie1 = fetch<MODE>(c, s - p.e, 1);
+  const WfRef de1 = fetch<MODE>(c, s - p.e, 2);
+  const WfRef mo2 = fetch<MODE>(c, s - c.o2 - c.e2, 0);
+  const WfRef ie2 = fetch<MODE>(c, s - c.e2, 3);
+  const WfRef de2 = fetch<MODE>(c, s - c.e2, 4);
   const bool hx = mx.nonnull(), ho1 = mo1.nonnull(), hie1 = ie1.nonnull(), hde1 = de1.nonnull();
   const bool ho2 = mo2.nonnull(), hie2 = ie2.nonnull(), hde2 = de2.nonnull();
   if (!hx && !ho1 && !hie1 && !hde1 && !ho2 && !hie2 && !hde2) {
@@ -589,9 +562,9 @@ __device__ __noinline__ int dir_step_2p(Dir& d, const Pen p, int s, const Grp<G>
   lo = min(lo, (hde2 ? de2.lo : 1) - 1);  hi = max(hi, (hde2 ? de2.hi : -1) - 1);
   const bool ai1 = ho1 || hie1, ad1 = ho1 || hde1, ai2 = ho2 || hie2, ad2 = ho2 || hde2;
   const int width = hi - lo + 1;
-  RefOf<MODE> om, oi1, od1, oi2, od2;
+  WfRef om, oi1, od1, oi2, od2;
   int offm = 0, offi1 = 0, offd1 = 0, offi2 = 0, offd2 = 0, need = 0;
-  if constexpr (!kLeaf) {
+  if (!kLeaf) {
     if (width > c.W) return -1;
     om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
     oi1.base = om.base + c.W;
@@ -672,7 +645,7 @@ __device__ __noinline__ int dir_step_2p(Dir& d, const Pen p, int s, const Grp<G>
     done = (ra[0] <= ak && ak <= ra[1]) && (om.at(ak) >= sv.tlen);
   } else {
     const int j = (ce == CI) ? 0 : (ce == CD) ? 1 : (ce == CI2) ? 2 : 3;
-    const RefOf<MODE>& t = (j == 0) ? oi1 : (j == 1) ? od1 : (j == 2) ? oi2 : od2;
+    const WfRef& t = (j == 0) ? oi1 : (j == 1) ? od1 : (j == 2) ? oi2 : od2;
     done = alloc[j] && (tlo[j] <= ak && ak <= thi[j]) && (t.at(ak) >= sv.tlen);
   }
   if (done) { d.status = ST_END_REACHED; d.status_score = s; d.end_k = ak; return 1; }
@@ -694,10 +667,10 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   const uint32_t tl = (uint32_t)sv.tlen, pl = (uint32_t)sv.plen;
   *max_ak_out = 0;
   if (kLeaf && s > c.lmax) return -1;
-  const RefOf<MODE> mx = fetch<MODE>(c, s - p.x, 0);
-  const RefOf<MODE> mo = fetch<MODE>(c, s - p.o - p.e, 0);
-  const RefOf<MODE> ie = lin ? absent_ref<RefOf<MODE>>() : fetch<MODE>(c, s - p.e, 1);
-  const RefOf<MODE> de = lin ? absent_ref<RefOf<MODE>>() : fetch<MODE>(c, s - p.e, 2);
+  const WfRef mx = fetch<MODE>(c, s - p.x, 0);
+  const WfRef mo = fetch<MODE>(c, s - p.o - p.e, 0);
+  const WfRef ie = lin ? absent_ref() : fetch<MODE>(c, s - p.e, 1);
+  const WfRef de = lin ? absent_ref() : fetch<MODE>(c, s - p.e, 2);
   const bool hx = mx.nonnull(), ho = mo.nonnull(), hie = ie.nonnull(), hde = de.nonnull();
   if (!hx && !ho && !hie && !hde) {
     // null step: no wavefront; the extension finds no M (wavefront_extend_end2end)
@@ -717,9 +690,9 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
   }
   const bool ai = !lin && (ho || hie), ad = !lin && (ho || hde);
   const int width = hi - lo + 1;
-  RefOf<MODE> om, oi, od;
+  WfRef om, oi, od;
   int offm = 0, offi = 0, offd = 0, need = 0;
-  if constexpr (!kLeaf) {
+  if (!kLeaf) {
     if (width > c.W) return -1;
     om.base = c.rdata + (size_t)(nphys * 3 + 0) * c.W;
     oi.base = om.base + c.W;
@@ -804,7 +777,7 @@ __device__ __noinline__ int dir_step(Dir& d, const Pen p, int s, const Grp<G> g,
     done = (r[0] <= ak && ak <= r[1]) && (om.at(ak) >= sv.tlen);
   } else {
     const bool alloc = (ce == CI) ? ai : ad;
-    const RefOf<MODE>& t = (ce == CI) ? oi : od;
+    const WfRef& t = (ce == CI) ? oi : od;
     const int tlo = (ce == CI) ? r[2] : r[4], thi = (ce == CI) ? r[3] : r[5];
     done = alloc && (tlo <= ak && ak <= thi) && (t.at(ak) >= sv.tlen);
   }
@@ -818,7 +791,7 @@ struct BP { int score, sf, sr, kf, kr, of, orv, comp; };
 // wavefront_bialign_breakpoint_indel2indel / _m2m: the first k0 (ascending) that meets,
 // found with a ballot per 32 diagonals (and the lowest hitting warp for G > 1).
 template <int G>
-__device__ void bp_scan(bool is_m, bool fwd, int s0, int s1, const RingRef& w0, const RingRef& w1,
+__device__ void bp_scan(bool is_m, bool fwd, int s0, int s1, const WfRef& w0, const WfRef& w1,
                         int plen, int tlen, int go, int comp, BP& bp, const Grp<G> g) {
   const int lo0 = w0.lo, hi0 = w0.hi;
   const int lo1 = tlen - plen - w1.hi, hi1 = tlen - plen - w1.lo;
@@ -871,23 +844,23 @@ __device__ __noinline__ void overlap_2p(const Dir& d0, const Dir& d1, int s0, in
                                         const Grp<G> g) {
   const DirCfg c0 = d0.cfg, c1 = d1.cfg;
   const int plen = d0.sv.plen, tlen = d0.sv.tlen, o2 = c0.o2;
-  const RingRef m0 = ref_raw<0>(c0, s0, 0);
+  const WfRef m0 = ref_raw<0>(c0, s0, 0);
   if (!m0.present()) return;
   for (int i = 0; i < p.scope; ++i) {
     const int si = s1 - i;
     if (si < 0) break;
     if (s0 + si - o2 >= bp.score) continue;
-    const RingRef dd20 = ref_raw<0>(c0, s0, 4), dd21 = ref_raw<0>(c1, si, 4);
+    const WfRef dd20 = ref_raw<0>(c0, s0, 4), dd21 = ref_raw<0>(c1, si, 4);
     if (dd20.present() && dd21.present()) bp_scan<G>(false, fwd, s0, si, dd20, dd21, plen, tlen, o2, CD2, bp, g);
-    const RingRef ii20 = ref_raw<0>(c0, s0, 3), ii21 = ref_raw<0>(c1, si, 3);
+    const WfRef ii20 = ref_raw<0>(c0, s0, 3), ii21 = ref_raw<0>(c1, si, 3);
     if (ii20.present() && ii21.present()) bp_scan<G>(false, fwd, s0, si, ii20, ii21, plen, tlen, o2, CI2, bp, g);
     if (s0 + si - p.o >= bp.score) continue;
-    const RingRef dd0 = ref_raw<0>(c0, s0, 2), dd1 = ref_raw<0>(c1, si, 2);
+    const WfRef dd0 = ref_raw<0>(c0, s0, 2), dd1 = ref_raw<0>(c1, si, 2);
     if (dd0.present() && dd1.present()) bp_scan<G>(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, g);
-    const RingRef ii0 = ref_raw<0>(c0, s0, 1), ii1 = ref_raw<0>(c1, si, 1);
+    const WfRef ii0 = ref_raw<0>(c0, s0, 1), ii1 = ref_raw<0>(c1, si, 1);
     if (ii0.present() && ii1.present()) bp_scan<G>(false, fwd, s0, si, ii0, ii1, plen, tlen, p.o, CI, bp, g);
     if (s0 + si >= bp.score) continue;
-    const RingRef mm1 = ref_raw<0>(c1, si, 0);
+    const WfRef mm1 = ref_raw<0>(c1, si, 0);
     if (mm1.present()) bp_scan<G>(true, fwd, s0, si, m0, mm1, plen, tlen, p.o, CM, bp, g);
   }
 }
@@ -900,20 +873,20 @@ __device__ __noinline__ void overlap(const Dir& d0, const Dir& d1, int s0, int s
   if (TWO) { overlap_2p<G>(d0, d1, s0, s1, fwd, bp, p, g); return; }
   const DirCfg c0 = d0.cfg, c1 = d1.cfg;
   const int plen = d0.sv.plen, tlen = d0.sv.tlen;
-  const RingRef m0 = ref_raw<0>(c0, s0, 0);
+  const WfRef m0 = ref_raw<0>(c0, s0, 0);
   if (!m0.present()) return;
-  const RingRef dd0 = ref_raw<0>(c0, s0, 2);
-  const RingRef ii0 = ref_raw<0>(c0, s0, 1);
+  const WfRef dd0 = ref_raw<0>(c0, s0, 2);
+  const WfRef ii0 = ref_raw<0>(c0, s0, 1);
   for (int i = 0; i < p.scope; ++i) {
     const int si = s1 - i;
     if (si < 0) break;
     if (s0 + si - p.go >= bp.score) continue;
-    const RingRef dd1 = ref_raw<0>(c1, si, 2);
+    const WfRef dd1 = ref_raw<0>(c1, si, 2);
     if (dd0.present() && dd1.present()) bp_scan<G>(false, fwd, s0, si, dd0, dd1, plen, tlen, p.o, CD, bp, g);
-    const RingRef ii1 = ref_raw<0>(c1, si, 1);
+    const WfRef ii1 = ref_raw<0>(c1, si, 1);
     if (ii0.present() && ii1.present()) bp_scan<G>(false, fwd, s0, si, ii0, ii1, plen, tlen, p.o, CI, bp, g);
     if (s0 + si >= bp.score) continue;
-    const RingRef mm1 = ref_raw<0>(c1, si, 0);
+    const WfRef mm1 = ref_raw<0>(c1, si, 0);
     if (mm1.present()) bp_scan<G>(true, fwd, s0, si, m0, mm1, plen, tlen, p.o, CM, bp, g);
   }
 }
@@ -954,8 +927,8 @@ __device__ __noinline__ int find_breakpoint(Dir& F, Dir& R, const PairSeqs& q, i
   const int guard = score_guard(p, plen, tlen);
   int sf = 0, sr = 0, fmax = 0, rmax = 0, ak = 0;
   bp.score = INT_MAX;
-  if (dir_extend<G, 0>(F, sf, g, &fmax)) return F.status;
-  if (dir_extend<G, 0>(R, sr, g, &rmax)) return R.status;
+  if (dir_extend<G>(F, sf, g, &fmax)) return F.status;
+  if (dir_extend<G>(R, sr, g, &rmax)) return R.status;
   bool last_fwd = false;
   for (;;) {
     if (fmax + rmax >= max_antidiag) break;
@@ -1156,7 +1129,7 @@ __device__ __noinline__ int leaf_align(Dir& B, const PairSeqs& q, int pb, int pe
   g.sync();
   const int guard = score_guard(p, pe - pb, te - tb);
   int s = 0, ak = 0;
-  if (!dir_extend<G, 1>(B, s, g, nullptr)) {
+  if (!dir_extend<G>(B, s, g, nullptr)) {
     for (;;) {
       ++s;
       // wavefront_unialign_reached_limits checks the step count after compute, before extend
@@ -1234,8 +1207,7 @@ __global__ void __launch_bounds__(G * GROUPS * 32, MINB) biwfa_persistent_kernel
                                          P.run_cap, P.leaf_run_cap, P.stack_cap, nc);
   uint8_t* arena = P.arena + ggroup * P.arena_bytes;
   const size_t ring_dir = (size_t)nphys * nc * P.ring_w;
-  ring_t* ring = RING_SMEM ? reinterpret_cast<ring_t*>(s_ring_dyn) + (size_t)gib * 2 * ring_dir
-                           : reinterpret_cast<ring_t*>(arena + L.ring_off);
+  int32_t* ring = RING_SMEM ? s_ring_dyn + (size_t)gib * 2 * ring_dir : (int32_t*)(arena + L.ring_off);
   int4* ldesc = (int4*)(arena + L.ldesc_off);
   int32_t* ldata = (int32_t*)(arena + L.ldata_off);
   uint32_t* runs = (uint32_t*)(arena + L.runs_off);
