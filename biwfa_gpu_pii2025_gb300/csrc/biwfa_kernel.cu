@@ -64,7 +64,7 @@ constexpr int kStepUnroll = WFG_STEP_UNROLL;        // diagonals per thread per 
 // 1 kbp pairs 6.7 %, 150 bp pairs 4.3 %, uneven pairs 2.4 %, two-piece equal, edit 2.8 %
 // slower; three diagonals 3.5 % slower on the mixture. In the ring steps two per thread stay
 // best (one 4.3 %, three 8.7 % slower). The multi-warp shapes keep two in the leaf steps (the
-// 50-100 kbp pairs on 8-warp groups: 28.8 s with two, 30.5 s with one).
+// 50-100 kbp pairs on 8-warp groups measured 1.5 % slower with one).
 constexpr int kLeafUnroll = WFG_LEAF_UNROLL;
 constexpr int ST_OK = -1, ST_END_REACHED = -2, ST_END_UNREACHABLE = -3;
 constexpr int CM = 0, CI = 1, CI2 = 2, CD = 3, CD2 = 4;  // components (affine2p_matrix_type values)
