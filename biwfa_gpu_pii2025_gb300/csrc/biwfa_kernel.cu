@@ -150,6 +150,13 @@ __device__ __forceinline__ uint32_t win32(const uint32_t* w, int pos, int bshift
 #ifndef WFG_ALIGN_START
 #define WFG_ALIGN_START 0
 #endif
+// 8-warp shape with HBM rings (the retry passes, the sorted schedule's longest pairs): blocks
+// per SM. Four (32 warps, 64 registers) measured on the 2,000 pairs of 50-100 kbp at 12 %
+// (same GB300, identical results): 23.2 s, against 25.4 s with three (80 registers) and 28.9 s
+// with two (127 registers, no spills).
+#ifndef WFG_G8_MIN_BLOCKS
+#define WFG_G8_MIN_BLOCKS 4
+#endif
 
 #if WFG_LCP64 >= 1
 // 64-bit window (32 bases of a 2-bit pair, 8 bytes of an 8-bit one) starting at character
@@ -1485,7 +1492,7 @@ cudaError_t occupancy_shape(int gw, int ring_in_smem, size_t dyn, int* blocks_pe
   if (gw <= 1) return occupancy_of<1, kG1Groups, false, g1_min_blocks<TWO>(), TWO, MS>(kSeqSmemBytesG1, blocks_per_sm);
   if (gw == 8) {
     if (ring_in_smem) return occupancy_of<8, 1, true, 1, TWO, MS>(dyn, blocks_per_sm);
-    return occupancy_of<8, 1, false, 2, TWO, MS>(0, blocks_per_sm);
+    return occupancy_of<8, 1, false, WFG_G8_MIN_BLOCKS, TWO, MS>(0, blocks_per_sm);
   }
   if (ring_in_smem) return occupancy_of<4, 1, true, 1, TWO, MS>(dyn, blocks_per_sm);
   return occupancy_of<4, 1, false, 3, TWO, MS>(0, blocks_per_sm);
@@ -1497,7 +1504,7 @@ cudaError_t launch_kernel(const KernelParams& p, int grid, cudaStream_t stream) 
   if (gw == 1) return launch_shape<1, kG1Groups, false, g1_min_blocks<TWO>(), TWO, MS>(p, grid, stream);
   if (gw == 8) {
     if (p.ring_in_smem) return launch_shape<8, 1, true, 1, TWO, MS>(p, grid, stream);
-    return launch_shape<8, 1, false, 2, TWO, MS>(p, grid, stream);
+    return launch_shape<8, 1, false, WFG_G8_MIN_BLOCKS, TWO, MS>(p, grid, stream);
   }
   if (gw == 4) {
     if (p.ring_in_smem) return launch_shape<4, 1, true, 1, TWO, MS>(p, grid, stream);
