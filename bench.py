@@ -225,6 +225,26 @@ CPU_NOTE = {"reference": "WFA2-lib v2.3 BiWFA itself (ultralow memory, heuristic
                     "were not present on this machine)"}
 
 
+def host_cpu() -> str:
+    """The host's CPU model as the system reports it (lscpu's model name, else /proc/cpuinfo's),
+    with the machine type; only the machine type where neither is readable."""
+    import platform
+    arch = platform.machine() or "unknown"
+    name = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        name = next((ln.split(":", 1)[1].strip() for ln in out.splitlines() if ln.startswith("Model name:")), "")
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not name:
+        try:
+            with open("/proc/cpuinfo") as f:
+                name = next((ln.split(":", 1)[1].strip() for ln in f if ln.lower().startswith("model name")), "")
+        except OSError:
+            pass
+    return f"{name} ({arch})" if name else arch
+
+
 def cpu_baseline(batch, workload: int = 5, threads: int | None = None, metric: int = 0, penalties=PENALTIES):
     """The CPU reference on all host cores over the workload's fixed sample (one warm pass,
     then the timed pass)."""
@@ -233,7 +253,7 @@ def cpu_baseline(batch, workload: int = 5, threads: int | None = None, metric: i
     cpu_time(sub, threads, penalties, metric)
     secs, kind, _, _ = cpu_time(sub, threads, penalties, metric)
     cells = float((sub.plen.astype(np.float64) * sub.tlen).sum())
-    out = {"value": m / secs, "unit": "pairs/s", "cores": threads, "kind": kind,
+    out = {"value": m / secs, "unit": "pairs/s", "cores": threads, "kind": kind, "cpu": host_cpu(),
            "sample": f"{m} pairs drawn uniformly (seed 99) from the same batch; {secs:.2f} s wall",
            "gcups": cells / secs / 1e9, "implementation": CPU_NOTE[kind]}
     if kind == "port":
@@ -289,7 +309,7 @@ def run_reference(args):
             "config": {"workload": name, "num_pairs": n, "sample_pairs_per_step": m, "seed": SEED,
                        "penalties": list(PENALTIES)},
             "gcups": cells * args.steps / t / 1e9,
-            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": kind,
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": kind, "cpu": host_cpu(),
                              "sample": f"{m} pairs per step drawn uniformly (seed 99) from the batch"},
             "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": CPU_NOTE[kind] + "; all host threads, the same sample as the GPU run's cpu_baseline"}
